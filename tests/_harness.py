@@ -1,0 +1,178 @@
+"""Shared helpers of the test-suite: loading the CPU oracle, building inputs, running the
+reference's known-answer cases through either the oracle or the GPU library.
+
+The oracle (oracle/modle_oracle.cpp) is test infrastructure: it is only loaded here, by
+__graft_entry__.smoke() and by the CPU-baseline leg of bench.py.
+"""
+
+import ctypes as C
+import json
+import os
+import subprocess
+
+import numpy as np
+
+from modlefork_gb300 import _abi as abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+U64MAX = (1 << 64) - 1
+
+_oracle = None
+
+
+def load_oracle():
+    """Load (building first if needed) the CPU oracle library."""
+    global _oracle
+    if _oracle is not None:
+        return _oracle
+    if not os.path.exists(ORACLE_SO):
+        subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
+    lib = C.CDLL(ORACLE_SO)
+    P = C.POINTER
+    lib.orc_config_defaults.argtypes = [P(abi.Config)]
+    lib.orc_config_transform.argtypes = [P(abi.Config)]
+    lib.orc_config_transform.restype = C.c_int
+    lib.orc_num_lefs.argtypes = [P(abi.Config), C.c_uint64]
+    lib.orc_num_lefs.restype = C.c_uint64
+    lib.orc_contacts_per_epoch.argtypes = [P(abi.Config), C.c_uint64]
+    lib.orc_contacts_per_epoch.restype = C.c_uint64
+    lib.orc_task_targets.argtypes = [P(abi.Config), C.c_uint64, C.c_uint64, C.c_uint64,
+                                     P(C.c_uint64), P(C.c_uint64)]
+    lib.orc_task_targets.restype = C.c_int
+    lib.orc_prng_seed.argtypes = [C.c_uint64, P(C.c_uint64)]
+    lib.orc_prng_draws.argtypes = [C.c_uint64, C.c_uint64, P(C.c_uint64)]
+    lib.orc_sample.argtypes = [C.c_uint64, C.c_int, C.c_uint64, C.c_uint64, C.c_double,
+                               C.c_double, C.c_uint64, P(C.c_double)]
+    lib.orc_sample.restype = C.c_uint64
+    lib.orc_simulate_cell.argtypes = [P(abi.Config), P(abi.Chrom), P(abi.Barrier), C.c_uint64,
+                                      C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64,
+                                      P(C.c_uint32), P(abi.CellStats), P(abi.TraceRequest)]
+    lib.orc_simulate_cell.restype = C.c_int
+    lib.orc_simulate_cells_mt.argtypes = [P(abi.Config), P(abi.Chrom), P(abi.Barrier),
+                                          C.c_uint64, P(C.c_uint64), P(C.c_uint64),
+                                          C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64,
+                                          P(C.c_uint32), P(C.c_uint64), P(abi.CellStats)]
+    lib.orc_simulate_cells_mt.restype = C.c_int
+    lib.orc_state_digest.argtypes = [C.c_uint64] + [P(C.c_uint64)] * 9
+    lib.orc_state_digest.restype = C.c_uint64
+    lib.orc_run_phase.argtypes = [P(abi.Config), P(abi.Chrom), P(abi.Barrier), C.c_uint64,
+                                  C.c_int, P(abi.PhaseIO)]
+    lib.orc_run_phase.restype = C.c_int
+    _oracle = lib
+    return lib
+
+
+def oracle_config(overrides=None, transform=False):
+    lib = load_oracle()
+    cfg = abi.Config()
+    lib.orc_config_defaults(C.byref(cfg))
+    for k, v in (overrides or {}).items():
+        setattr(cfg, k, v)
+    if transform:
+        rc = lib.orc_config_transform(C.byref(cfg))
+        assert rc == 0
+    return cfg
+
+
+def make_chrom(start, end, size=None, name=b"chr1"):
+    ch = abi.Chrom()
+    ch.name = name
+    ch.name_len = len(name)
+    ch.size = size if size is not None else end
+    ch.start = start
+    ch.end = end
+    return ch
+
+
+class PhaseState:
+    """Numpy-backed state of one cell in the reference's encodings (mgpu_phase_io)."""
+
+    def __init__(self, lefs, rev_ranks, fwd_ranks, rev_moves, fwd_moves, released=(),
+                 barrier_states=None, seed=0, prng_state=None):
+        n = len(lefs)
+        self.n = n
+        self.rev_pos = np.array([l[0] for l in lefs], dtype=np.uint64)
+        self.fwd_pos = np.array([l[1] for l in lefs], dtype=np.uint64)
+        self.binding_epoch = np.array([l[2] for l in lefs], dtype=np.uint64)
+        for i in released:
+            self.rev_pos[i] = U64MAX
+            self.fwd_pos[i] = U64MAX
+            self.binding_epoch[i] = U64MAX
+        self.rev_rank = np.array(rev_ranks, dtype=np.uint64)
+        self.fwd_rank = np.array(fwd_ranks, dtype=np.uint64)
+        self.rev_move = np.array(rev_moves, dtype=np.uint64)
+        self.fwd_move = np.array(fwd_moves, dtype=np.uint64)
+        self.rev_collision = np.zeros(n, dtype=np.uint64)
+        self.fwd_collision = np.zeros(n, dtype=np.uint64)
+        self.bind_mask = None
+        self.barrier_state = (np.array(barrier_states, dtype=np.uint8)
+                              if barrier_states is not None else None)
+        self.prng = (list(prng_state) if prng_state is not None
+                     else list(prng_state_from_seed(seed)))
+        self.n5 = self.n3 = self.released = 0
+
+    def io(self, **kw):
+        io = abi.PhaseIO()
+        io.num_lefs = self.n
+        for name in abi.TRACE_ARRAYS:
+            setattr(io, name, abi.ptr64(getattr(self, name)))
+        io.bind_mask = abi.ptr64(self.bind_mask)
+        if self.barrier_state is not None:
+            io.barrier_state = self.barrier_state.ctypes.data_as(C.POINTER(C.c_uint8))
+        for k, v in kw.items():
+            setattr(io, k, v)
+        for k in range(4):
+            io.prng_state[k] = self.prng[k]
+        return io
+
+    def absorb(self, io):
+        self.prng = [io.prng_state[k] for k in range(4)]
+        self.n5, self.n3, self.released = io.n5prime, io.n3prime, io.lefs_released
+
+
+def prng_state_from_seed(seed):
+    lib = load_oracle()
+    st = (C.c_uint64 * 4)()
+    lib.orc_prng_seed(C.c_uint64(seed), st)
+    return [st[i] for i in range(4)]
+
+
+def load_golden_cases():
+    with open(os.path.join(GOLDEN, "reference_unit_tests.json")) as f:
+        return json.load(f)["cases"]
+
+
+def golden_inputs(case):
+    """(config overrides, chromosome, barrier dicts, PhaseState) of one golden case."""
+    chrom = case["chrom"] or {"start": 0, "end": (1 << 32) - 2, "size": (1 << 32) - 2}
+    st = PhaseState(case["lefs"], case["rev_ranks"], case["fwd_ranks"], case["rev_moves"],
+                    case["fwd_moves"], case["released"],
+                    [b["state"] for b in case["barriers"]], seed=case["seed"])
+    return case["config"], chrom, case["barriers"], st
+
+
+def run_golden_case(case, run_phase):
+    """Run the hooks of a golden case through ``run_phase(phase_id, io) -> status``."""
+    _, _, _, st = golden_inputs(case)
+    for step in case["steps"]:
+        kw = {}
+        if step["hook"] == "RANK":
+            kw = dict(ranks_partially_sorted=step.get("partially_sorted", 1),
+                      init_ranks=step.get("init_ranks", 0))
+        io = st.io(**kw)
+        rc = run_phase(abi.PHASES[step["hook"]], io)
+        assert rc == 0, f"{case['name']}: {step['hook']} returned {rc}"
+        st.absorb(io)
+    return st
+
+
+def check_golden(case, st):
+    exp = case["expected"]
+    out = {"rev_moves": st.rev_move, "fwd_moves": st.fwd_move,
+           "rev_collisions": st.rev_collision, "fwd_collisions": st.fwd_collision,
+           "rev_ranks": st.rev_rank, "fwd_ranks": st.fwd_rank}
+    for key, want in exp.items():
+        got = [int(x) for x in out[key]]
+        assert got == [int(x) for x in want], f"{case['name']} {key}: got {got} want {want}"
