@@ -1,0 +1,362 @@
+#!/usr/bin/env python3
+"""Benchmark of the loop-extrusion epoch engine on the genome-scale workload.
+
+Workload (one step): 24 synthetic chromosomes, lengths uniform in [50, 250] Mbp, 5 kb bins,
+3 Mbp band, one barrier per 50 kb (Beta(8, 2) occupancy), 20 LEFs/Mbp, 200 kb lifetime,
+512 cells per chromosome, contact density 1, one engine launch per chromosome.  The
+metric is LEF-epochs/s (sum over cells and epochs of active LEFs, burn-in included), with
+cells/s and contacts/s reported beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``value`` is timed with CUDA events around K steps whose inputs (seeds, targets, bands)
+are already in device memory; ``e2e`` repeats the step through the C ABI with host buffers
+(host-to-device copies of the inputs and the band, device-to-host copies of the band and the
+per-cell statistics inside the timed region).  ``--impl reference`` times the reference
+algorithm on the host cores instead (the CPU oracle, a restatement of the reference, since
+the reference's own build needs dependencies this machine does not have) on a bounded sample
+of the same workload.
+"""
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "genome_24chr_50-250Mbp_5kb_512cells"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cells", type=int, default=512, help="cells per chromosome")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline time budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------------------------
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region (SM clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[4:]))
+            except ValueError:
+                continue
+        os.remove(self.path)
+        if not rows:
+            return None
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = set()
+        for _, _, flags in rows:
+            for name, v in zip(names[1:], flags[1:]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dram_traffic_per_launch():
+    """DRAM bytes per launch of the simulation kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "simulate_kernel_traffic.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get("bytes_per_launch"), d
+    return None, None
+
+
+# ---------------------------------------------------------------------------------------------
+def build_workload(cells, rank):
+    from modlefork_gb300 import engine, genome
+
+    cfg, gen = genome.genome_24chr(seed=11)
+    tasks = []
+    for chrom, bars in gen:
+        size = chrom.simulated_size
+        nl = engine.num_lefs(cfg, size)
+        targets, te = engine.task_targets(cfg, size, nl, cells)
+        base = rank * cells  # weak scaling: each rank simulates its own cell ids
+        seeds = np.array([engine.cell_seed(chrom.name, chrom.size, cfg.seed, base + i) for i in range(cells)],
+                         dtype=np.uint64)
+        nrows, ncols = engine.band_shape(cfg, size)
+        tasks.append(dict(chrom=chrom, bars=bars, nlefs=nl, targets=targets, te=te, seeds=seeds,
+                          nrows=nrows, ncols=ncols))
+    return cfg, tasks
+
+
+def algorithmic_bytes(stats, nbarriers):
+    """B_epoch = 24 A + 6 N_b + 8 C summed over the cell-epochs of one launch."""
+    lef_epochs = sum(s.lef_epochs for s in stats)
+    epochs = sum(s.epochs for s in stats)
+    contacts = sum(s.contacts for s in stats)
+    return 24 * lef_epochs + 6 * nbarriers * epochs + 8 * contacts
+
+
+def cpu_sample(cfg, task, budget_s, threads):
+    """Time the oracle on whole cells of one chromosome with all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _harness import load_oracle, make_chrom
+    from modlefork_gb300 import _abi as abi
+
+    lib = load_oracle()
+    chrom = task["chrom"]
+    bs = abi.make_barriers(task["bars"])
+    ch = make_chrom(chrom.start, chrom.end, chrom.size, chrom.name.encode())
+    band = np.zeros(task["nrows"] * task["ncols"], dtype=np.uint32)
+    done_cells = lef_epochs = contacts = 0
+    t0 = time.perf_counter()
+    i0 = 0
+    while time.perf_counter() - t0 < budget_s and i0 < len(task["seeds"]):
+        n = min(threads, len(task["seeds"]) - i0)
+        st = (abi.CellStats * n)()
+        missed = C.c_uint64(0)
+        seeds = np.ascontiguousarray(task["seeds"][i0:i0 + n])
+        targets = np.ascontiguousarray(task["targets"][i0:i0 + n])
+        rc = lib.orc_simulate_cells_mt(C.byref(cfg), C.byref(ch), bs, len(task["bars"]),
+                                       seeds.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                       targets.ctypes.data_as(C.POINTER(C.c_uint64)), task["te"],
+                                       task["nlefs"], n, threads,
+                                       band.ctypes.data_as(C.POINTER(C.c_uint32)), C.byref(missed), st)
+        if rc != 0:
+            raise RuntimeError(f"oracle failed with {rc}")
+        done_cells += n
+        lef_epochs += sum(s.lef_epochs for s in st)
+        contacts += sum(s.contacts for s in st)
+        i0 += n
+    dt = time.perf_counter() - t0
+    return dict(seconds=dt, cells=done_cells, lef_epochs=lef_epochs, contacts=contacts,
+                sample=f"{chrom.name} ({chrom.size / 1e6:.1f} Mbp, {task['nlefs']} LEFs, "
+                       f"{len(task['bars'])} barriers): cells 0..{done_cells - 1} of {len(task['seeds'])}, "
+                       f"{threads} threads")
+
+
+# ---------------------------------------------------------------------------------------------
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if world > 1 and rank != 0:
+        return
+    from modlefork_gb300 import build as mbuild
+
+    mbuild.build()
+    cfg, tasks = build_workload(args.cells, 0)
+    threads = os.cpu_count() or 1
+    per_step = max(1.0, args.cpu_seconds / 2)
+    for _ in range(args.warmup):
+        cpu_sample(cfg, tasks[0], 0.1, threads)  # one batch
+    rates, samples, secs = [], [], 0.0
+    for _ in range(args.steps):
+        s = cpu_sample(cfg, tasks[0], per_step, threads)
+        rates.append(s["lef_epochs"] / s["seconds"])
+        samples.append(s)
+        secs += s["seconds"]
+    value = sum(s["lef_epochs"] for s in samples) / secs
+    line = {
+        "impl": "reference", "metric": "LEF-epochs/s", "value": value, "unit": "LEF-epochs/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64+f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_per_step": samples[0]["sample"]},
+        "cpu_baseline": {"value": value, "unit": "LEF-epochs/s", "cores": threads, "kind": "port",
+                         "sample": samples[0]["sample"]},
+        "e2e": {"value": value, "unit": "LEF-epochs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cells_per_s": sum(s["cells"] for s in samples) / secs,
+        "contacts_per_s": sum(s["contacts"] for s in samples) / secs,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    from modlefork_gb300 import build as mbuild
+    from modlefork_gb300 import engine
+
+    mbuild.build()
+    cfg, tasks = build_workload(args.cells, rank)
+    eng = engine.Engine(cfg, local)
+    stream = torch.cuda.current_stream()
+    eng.set_stream(stream.cuda_stream)
+    dev = torch.device("cuda", local)
+    for t in tasks:
+        t["cid"] = eng.upload_chrom(t["chrom"], t["bars"])
+        t["d_seeds"] = torch.from_numpy(t["seeds"].view(np.int64)).to(dev)
+        t["d_targets"] = torch.from_numpy(t["targets"].view(np.int64)).to(dev)
+        t["d_band"] = torch.zeros(t["nrows"] * t["ncols"], dtype=torch.int32, device=dev)
+
+    def step(record):
+        tot = dict(lef_epochs=0, cells=0, contacts=0, bytes=0, kernel_ms=0.0, launches=0)
+        for t in tasks:
+            _, st = eng.simulate_cells(t["cid"], t["d_seeds"].data_ptr(), t["d_targets"].data_ptr(),
+                                       t["te"], t["nlefs"], t["d_band"].data_ptr())
+            if record:
+                tot["lef_epochs"] += sum(s.lef_epochs for s in st)
+                tot["contacts"] += sum(s.contacts for s in st)
+                tot["cells"] += len(st)
+                tot["bytes"] += algorithmic_bytes(st, len(t["bars"]))
+                tot["kernel_ms"] += eng.last_kernel_ms()
+                tot["launches"] += 1
+        return tot
+
+    for _ in range(args.warmup):
+        step(False)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    agg = dict(lef_epochs=0, cells=0, contacts=0, bytes=0, kernel_ms=0.0, launches=0)
+    for _ in range(args.steps):
+        s = step(True)
+        for k in agg:
+            agg[k] += s[k]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        import torch.distributed as dist
+
+        tm = torch.tensor([ms], device=dev)
+        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
+        ms = float(tm.item())
+        for k in ("lef_epochs", "cells", "contacts"):
+            v = torch.tensor([agg[k]], dtype=torch.float64, device=dev)
+            dist.all_reduce(v)
+            agg[k] = v.item()
+        dist.barrier()
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        host_bands = [np.zeros(t["nrows"] * t["ncols"], dtype=np.uint32) for t in tasks]
+        eng.set_stream(None)
+        torch.cuda.synchronize()
+        h2d = d2h = 0
+        le = 0
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            for t, hb in zip(tasks, host_bands):
+                _, st = eng.simulate_cells(t["cid"], t["seeds"], t["targets"], t["te"], t["nlefs"], hb)
+                le += sum(s.lef_epochs for s in st)
+                h2d += t["seeds"].nbytes + t["targets"].nbytes + hb.nbytes
+                d2h += hb.nbytes + len(st) * C.sizeof(st[0])
+        dt = time.perf_counter() - t0
+        e2e = {"value": le / dt, "unit": "LEF-epochs/s", "h2d_bytes_per_step": h2d // args.e2e_steps,
+               "d2h_bytes_per_step": d2h // args.e2e_steps}
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    achieved = agg["bytes"] / (agg["kernel_ms"] / 1e3) / 1e9
+    traffic, _ = dram_traffic_per_launch()
+    line = {
+        "metric": "LEF-epochs/s", "value": agg["lef_epochs"] / (ms / 1e3), "unit": "LEF-epochs/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32+f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "chromosomes": len(tasks), "cells_per_chromosome": args.cells,
+                   "genome_bp": int(sum(t["chrom"].size for t in tasks)),
+                   "lefs": int(sum(t["nlefs"] for t in tasks)),
+                   "barriers": int(sum(len(t["bars"]) for t in tasks)),
+                   "l2": "inputs larger than L2 (contact bands total "
+                         f"{sum(t['nrows'] * t['ncols'] * 4 for t in tasks) / 1e9:.2f} GB)"},
+        "cells_per_s": agg["cells"] / (ms / 1e3), "contacts_per_s": agg["contacts"] / (ms / 1e3),
+        "gpu_launches": agg["launches"] * world,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": f"{peak_kind} hbm_gbs", "kernel": "simulate_kernel",
+                     "bytes_model": "24*LEF_epochs + 6*barriers*epochs + 8*contacts per launch"},
+        "e2e": e2e, "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        s = cpu_sample(cfg, tasks[0], args.cpu_seconds, threads)
+        line["cpu_baseline"] = {"value": s["lef_epochs"] / s["seconds"], "unit": "LEF-epochs/s",
+                                "cores": threads, "kind": "port", "sample": s["sample"]}
+    print(json.dumps(line), flush=True)
+    eng.close()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -218,6 +218,12 @@ int mgpu_destroy(mgpu_ctx* ctx);
 /* Wait for every call issued on the context's stream. */
 int mgpu_sync(mgpu_ctx* ctx);
 
+/* Instrumentation (no counterpart in the reference): launch on the caller's CUDA stream
+ * (a cudaStream_t, NULL = the context's own stream), and read the device time of the last
+ * simulation kernel measured with CUDA events around its launch. */
+int mgpu_set_stream(mgpu_ctx* ctx, void* cuda_stream);
+int mgpu_last_kernel_ms(mgpu_ctx* ctx, double* ms);
+
 /* Upload one chromosome and its barriers (sorted with mgpu_sort_barriers order); returns a
  * handle in *chrom_id.  Barriers are shared by every cell of the chromosome. */
 int mgpu_upload_chrom(mgpu_ctx* ctx, const mgpu_chrom* chrom, const mgpu_barrier* barriers,

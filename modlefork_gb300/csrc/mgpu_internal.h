@@ -1,0 +1,156 @@
+// Internal declarations shared by the host library (mgpu_host.cpp) and the device code
+// (mgpu_device.cu).  Nothing here is part of the C ABI.
+#pragma once
+#include <stdint.h>
+
+#include "../../include/mgpu_modle.h"
+
+#if defined(__CUDACC__)
+#define MGPU_HD __host__ __device__
+#else
+#define MGPU_HD
+#endif
+
+namespace mgpu {
+
+typedef uint32_t u32;
+typedef uint64_t u64;
+typedef int64_t i64;
+
+// Unbound unit / LEF sentinel for the 32-bit device encodings.
+constexpr u32 UNBOUND = 0xFFFFFFFFu;
+
+// PRNG ring: each of the 32 lanes of a cell's warp generates RNG_S consecutive draws of the
+// cell's single Xoshiro256++ stream per refill; RING is a power of two holding two blocks.
+constexpr int RNG_S = 16;
+constexpr int RNG_BLOCK = 32 * RNG_S;
+constexpr int RING = 2 * RNG_BLOCK;
+constexpr int JUMP_DISTANCE = 31 * RNG_S;  // lane state advance between two refills
+constexpr int JUMP_TABLE_ENTRIES = 64 * 16;  // 4-bit chunks of the 256-bit state
+
+// Compact 32-bit collision word: event bits (collision_encoding.hpp:91-96) in bits 27..31,
+// index in bits 0..26.
+constexpr u32 CW_SHIFT = 27;
+constexpr u32 CW_IDX_MASK = (1u << CW_SHIFT) - 1;
+constexpr u32 EV_COLLISION = 0x10, EV_CHROM_BOUNDARY = 0x08, EV_LEF_BAR = 0x04,
+              EV_PRIMARY = 0x02, EV_SECONDARY = 0x01;
+
+MGPU_HD inline u32 cw_make(u32 idx, u32 ev) { return (idx & CW_IDX_MASK) | (ev << CW_SHIFT); }
+MGPU_HD inline u32 cw_idx(u32 w) { return w & CW_IDX_MASK; }
+MGPU_HD inline u32 cw_event(u32 w) { return w >> CW_SHIFT; }
+MGPU_HD inline bool cw_occurred(u32 w) { return (w >> CW_SHIFT) & EV_COLLISION; }
+MGPU_HD inline bool cw_occurred_as(u32 w, u32 c) { return (w >> CW_SHIFT) == (c | EV_COLLISION); }
+MGPU_HD inline bool cw_avoided_as(u32 w, u32 c) { return !cw_occurred(w) && (w >> CW_SHIFT) == c; }
+// reference 64-bit word: idx | event << 56
+MGPU_HD inline u64 cw_to_ref(u32 w) { return (u64)(w & CW_IDX_MASK) | ((u64)(w >> CW_SHIFT) << 56); }
+MGPU_HD inline u32 cw_from_ref(u64 w) {
+  return (u32)(w & CW_IDX_MASK) | ((u32)((w >> 56) & 0x1F) << CW_SHIFT);
+}
+
+// Barrier as seen by the kernels: integer thresholds replace the floating-point tests of
+// init_states (bernoulli), next_state (generate_canonical > stp).
+enum : u32 {
+  BF_DIR_MASK = 3u,        // MGPU_DIR_REV / MGPU_DIR_FWD
+  BF_OCC_DRAWS = 1u << 2,  // occupancy != 0: init_states draws for this barrier
+  BF_INA_NEVER = 1u << 3,  // no draw can make a free barrier occupied
+  BF_ACT_NEVER = 1u << 4,  // no draw can make an occupied barrier free
+};
+struct DevBarrier {
+  u64 t_occ;  // init: occupied iff draw <= t_occ
+  u64 t_ina;  // free -> occupied iff draw >= t_ina
+  u64 t_act;  // occupied -> free iff draw >= t_act
+  u32 pos;
+  u32 flags;
+};
+
+// Bernoulli trial with integer threshold: success iff draw <= thr; no draw when !draws.
+struct Trial {
+  u64 thr;
+  u32 draws;  // 0: p == 0, the reference returns false without drawing
+  u32 always; // 1: the reference short-circuits to true without drawing
+};
+
+struct KParams {
+  u32 start, end;  // simulated range [start, end)
+  u32 bin, nrows, ncols;
+  u32 nlefs, nbarriers;
+  u32 hist_cap, smooth_w;
+  u32 skip_burnin;
+  u64 min_burnin, max_burnin;
+  // moves: [0] = burn-in speeds, [1] = after burn-in
+  double rev_speed[2], fwd_speed[2];
+  double rev_std, fwd_std;
+  u64 rev_move_int[2], fwd_move_int[2];
+  // release_lefs: [burnin_completed][number of hard LEF-BAR collisions 0..2]
+  Trial release[2][3];
+  Trial lef_lef;      // run_lef_lef_collision_trial
+  Trial lef_bar[2];   // run_lef_bar_collision_trial: [0] major pblock, [1] minor pblock
+  // burn-in Poisson(nlefs / burnin_target_epochs) (constants computed on the host)
+  double pois_mean, pois_exp_mean, pois_smu, pois_b, pois_a, pois_inv_alpha, pois_v_r;
+  // contacts
+  u64 spe;               // sampling events per epoch
+  u32 contact_mode;      // target_contact_density >= 0
+  u32 density_positive;  // target_contact_density > 0
+  u32 ratio_mode;        // 0: all loop, 1: all TAD, 2: binomial split
+  u32 noisify;
+  double p_loop;         // 1 / (ratio + 1)
+  double gev_mu, gev_sigma, gev_xi;
+  // binomial(spe, p_loop) constants computed on the host
+  double bin_q_n;
+  // binding positions: uniform_int[start, end - 1]
+  u64 pos_bucket;
+  u64 pos_range;
+};
+
+struct CellTask {
+  u64 seed;
+  u64 target_contacts;
+};
+
+// Per-cell trace output (device pointers; all NULL when tracing is off).
+struct DevTrace {
+  u64 max_records;
+  mgpu_trace_header* headers;
+  u64 *rev_pos, *fwd_pos, *binding_epoch, *rev_rank, *fwd_rank, *rev_move, *fwd_move,
+      *rev_collision, *fwd_collision;
+  u64 max_epochs;
+  mgpu_trace_header* all_headers;
+  u64* num_recorded;
+};
+
+// Device error codes reported through mgpu_cell_stats::status (0 = OK).
+enum : u32 {
+  DEV_OK = 0,
+  DEV_ERR_ITER_LIMIT = 1,    // a rejection loop hit its iteration limit
+  DEV_ERR_MOVE_RANGE = 2,    // a move does not fit the 32-bit encoding
+  DEV_ERR_BAD_STATE = 3,     // the reference would read out of bounds here
+  DEV_ERR_NO_BOUND_LEF = 4,  // contact sampling found no bound LEF within bounds
+};
+
+// Shared-memory footprint of one cell.
+MGPU_HD inline u64 cell_smem_bytes(u64 nlefs, u64 nbarriers, u64 hist_cap) {
+  const u64 scalars = 512;
+  const u64 ring = (u64)RING * 8;
+  const u64 hist = 2 * hist_cap * 8;
+  const u64 bars = ((nbarriers + 31) / 32) * 4;
+  const u64 lefs = 10 * nlefs * 4;
+  return scalars + ring + hist + ((bars + 15) & ~15ull) + lefs;
+}
+
+// Host side helpers implemented in mgpu_host.cpp, device launchers in mgpu_device.cu.
+struct DevChrom {
+  const DevBarrier* barriers;
+  u32 nbarriers;
+};
+
+int launch_simulate(const KParams& P, const DevChrom& ch, const CellTask* tasks, u64 ncells,
+                    u64 target_epochs, u32* band, u64* missed, mgpu_cell_stats* stats,
+                    const DevTrace* trace, const void* jump_table, u32* work_counter,
+                    void* stream, char* errbuf, int errlen);
+int launch_phase(const KParams& P, const DevChrom& ch, int phase, u64 n, u64* arrays,
+                 u64* bind_mask, uint8_t* barrier_state, u64 epoch, u32 burnin_completed,
+                 u32 partially_sorted, u32 init_ranks, u32 adjust, u64* prng_state, u64* outs,
+                 const void* jump_table, void* stream, char* errbuf, int errlen);
+u64 max_smem_per_block();
+
+}  // namespace mgpu

@@ -1,0 +1,259 @@
+"""Python binding of the GB300 epoch engine (libmgpu_modle.so) through its C ABI.
+
+This mirrors the reference's operator interface for the hot path: ``Engine`` plays the role
+of ``modle::Simulation`` (src/libmodle/cpu/simulation.cpp:58-105) holding a transformed
+Config, and ``Engine.simulate_cells`` is the batched drop-in for calling
+``Simulation::simulate_one_cell`` once per (chromosome, cell) task
+(src/libmodle/cpu/scheduler_simulate.cpp:229-256).  Errors surface as ``EngineError`` with
+the library's status code and message; there is no CPU fallback: if the compiled library is
+missing, loading fails.
+"""
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi as abi
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libmgpu_modle.so")
+_lib = None
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{abi.STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load(path=LIB_PATH):
+    """Load the compiled engine; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: run modlefork_gb300.build.build() first")
+    lib = C.CDLL(path)
+    P = C.POINTER
+    u64, i32 = C.c_uint64, C.c_int
+    sigs = {
+        "mgpu_config_defaults": (None, [P(abi.Config)]),
+        "mgpu_config_transform": (i32, [P(abi.Config)]),
+        "mgpu_cell_seed": (u64, [C.c_char_p, u64, u64, u64, u64]),
+        "mgpu_xxh3_64": (u64, [C.c_void_p, u64, u64]),
+        "mgpu_num_lefs": (u64, [P(abi.Config), u64]),
+        "mgpu_contacts_per_epoch": (u64, [P(abi.Config), u64]),
+        "mgpu_npixels": (u64, [P(abi.Config), u64]),
+        "mgpu_band_shape": (None, [P(abi.Config), u64, P(u64), P(u64)]),
+        "mgpu_task_targets": (i32, [P(abi.Config), u64, u64, u64, P(u64), P(u64)]),
+        "mgpu_barrier_from_bed": (i32, [P(abi.Chrom), u64, u64, C.c_char, C.c_double, C.c_double,
+                                        C.c_double, P(abi.Barrier)]),
+        "mgpu_sort_barriers": (i32, [P(abi.Barrier), u64]),
+        "mgpu_last_error_string": (C.c_char_p, []),
+        "mgpu_abi_version": (i32, []),
+        "mgpu_create": (i32, [i32, P(abi.Config), P(C.c_void_p)]),
+        "mgpu_destroy": (i32, [C.c_void_p]),
+        "mgpu_sync": (i32, [C.c_void_p]),
+        "mgpu_upload_chrom": (i32, [C.c_void_p, P(abi.Chrom), P(abi.Barrier), u64, P(i32)]),
+        "mgpu_simulate_cells": (i32, [C.c_void_p, i32, C.c_void_p, C.c_void_p, u64, u64, u64,
+                                      C.c_void_p, C.c_void_p, C.c_void_p]),
+        "mgpu_trace_cell": (i32, [C.c_void_p, i32, u64, u64, u64, u64, C.c_void_p,
+                                  P(abi.CellStats), P(abi.TraceRequest)]),
+        "mgpu_state_digest": (u64, [u64] + [P(u64)] * 9),
+        "mgpu_run_phase": (i32, [C.c_void_p, i32, i32, P(abi.PhaseIO)]),
+        "mgpu_prng_seed": (None, [u64, P(u64)]),
+        "mgpu_set_stream": (i32, [C.c_void_p, C.c_void_p]),
+        "mgpu_last_kernel_ms": (i32, [C.c_void_p, P(C.c_double)]),
+    }
+    for name, (res, args) in sigs.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(rc, what=""):
+    if rc != abi.MGPU_OK:
+        msg = _lib.mgpu_last_error_string().decode(errors="replace")
+        raise EngineError(rc, f"{what}: {msg}" if what else msg)
+
+
+def config_defaults(**overrides):
+    """modle::Config defaults (simulation_config.hpp:24-135) with keyword overrides."""
+    lib = load()
+    cfg = abi.Config()
+    lib.mgpu_config_defaults(C.byref(cfg))
+    for k, v in overrides.items():
+        if not hasattr(cfg, k):
+            raise KeyError(k)
+        setattr(cfg, k, v)
+    return cfg
+
+
+def config_transform(cfg):
+    """Cli::transform_args (src/modle/cli.cpp:1194-1215), in place."""
+    lib = load()
+    _check(lib.mgpu_config_transform(C.byref(cfg)), "mgpu_config_transform")
+    return cfg
+
+
+def cell_seed(name, chrom_size, seed, cell_id):
+    """Chromosome::hash (src/libmodle/internal/genome.cpp:317-335)."""
+    lib = load()
+    b = name.encode() if isinstance(name, str) else bytes(name)
+    return lib.mgpu_cell_seed(b, len(b), chrom_size, seed, cell_id)
+
+
+def num_lefs(cfg, size_bp):
+    return load().mgpu_num_lefs(C.byref(cfg), size_bp)
+
+
+def band_shape(cfg, size_bp):
+    nr, nc = C.c_uint64(), C.c_uint64()
+    load().mgpu_band_shape(C.byref(cfg), size_bp, C.byref(nr), C.byref(nc))
+    return nr.value, nc.value
+
+
+def task_targets(cfg, size_bp, nlefs, ncells):
+    t = np.zeros(ncells, dtype=np.uint64)
+    e = C.c_uint64()
+    _check(load().mgpu_task_targets(C.byref(cfg), size_bp, nlefs, ncells,
+                                    t.ctypes.data_as(C.POINTER(C.c_uint64)), C.byref(e)),
+           "mgpu_task_targets")
+    return t, e.value
+
+
+def barriers_from_bed(chrom, records, default_stp_active, default_stp_inactive):
+    """BED records (start, end, strand, score) -> barrier list (genome.cpp:194-210)."""
+    lib = load()
+    ch = chrom.as_abi()
+    out = []
+    b = abi.Barrier()
+    for (s, e, strand, score) in records:
+        rc = lib.mgpu_barrier_from_bed(C.byref(ch), s, e, strand.encode(), float(score),
+                                       default_stp_active, default_stp_inactive, C.byref(b))
+        if rc < 0:
+            _check(rc, "mgpu_barrier_from_bed")
+        if rc == 1:
+            out.append(dict(pos=b.pos, stp_active=b.stp_active, stp_inactive=b.stp_inactive,
+                            blocking_dir=b.blocking_dir))
+    return out
+
+
+class Chromosome:
+    """Simulated range of one chromosome (modle::Chromosome)."""
+
+    def __init__(self, name, size, start=0, end=None):
+        self.name = name
+        self.size = int(size)
+        self.start = int(start)
+        self.end = int(size if end is None else end)
+
+    @property
+    def simulated_size(self):
+        return self.end - self.start
+
+    def as_abi(self):
+        ch = abi.Chrom()
+        self._name_bytes = self.name.encode()
+        ch.name = self._name_bytes
+        ch.name_len = len(self._name_bytes)
+        ch.size = self.size
+        ch.start = self.start
+        ch.end = self.end
+        return ch
+
+
+class Engine:
+    """A device context bound to one transformed Config (like modle::Simulation)."""
+
+    def __init__(self, cfg, device=0):
+        self.lib = load()
+        self.cfg = cfg
+        h = C.c_void_p()
+        _check(self.lib.mgpu_create(device, C.byref(cfg), C.byref(h)), "mgpu_create")
+        self.h = h
+        self.chroms = {}
+
+    def close(self):
+        if self.h:
+            self.lib.mgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def upload_chrom(self, chrom, barriers):
+        """Upload a chromosome and its barriers (IITree order); returns the handle."""
+        ch = chrom.as_abi()
+        bs = abi.make_barriers(barriers)
+        cid = C.c_int()
+        _check(self.lib.mgpu_upload_chrom(self.h, C.byref(ch), bs, len(barriers), C.byref(cid)),
+               "mgpu_upload_chrom")
+        self.chroms[cid.value] = chrom
+        return cid.value
+
+    def simulate_cells(self, chrom_id, seeds, targets, target_epochs, nlefs, band=None,
+                       stats=True):
+        """Simulate len(seeds) cells; contacts are added into ``band`` (numpy uint32 array or
+        device pointer).  Returns (missed_updates, per-cell stats array or None)."""
+        seeds = np.ascontiguousarray(seeds, dtype=np.uint64)
+        targets = np.ascontiguousarray(targets, dtype=np.uint64)
+        n = len(seeds)
+        missed = C.c_uint64(0)
+        st = (abi.CellStats * n)() if stats else None
+        if isinstance(band, np.ndarray):
+            assert band.dtype == np.uint32 and band.flags["C_CONTIGUOUS"]
+            band_ptr = band.ctypes.data
+        else:
+            band_ptr = band
+        _check(self.lib.mgpu_simulate_cells(self.h, chrom_id, seeds.ctypes.data, targets.ctypes.data,
+                                            target_epochs, nlefs, n, band_ptr,
+                                            C.addressof(missed), C.addressof(st) if st else None),
+               "mgpu_simulate_cells")
+        return missed.value, st
+
+    def trace_cell(self, chrom_id, seed, target, target_epochs, nlefs, max_records=0,
+                   max_epochs=0, band=None):
+        """Run one cell recording per-epoch state; returns (stats, headers, arrays, all_headers)."""
+        tr = abi.TraceRequest()
+        tr.max_records = max_records
+        arrays = {}
+        headers = (abi.TraceHeader * max(1, max_records))()
+        if max_records:
+            tr.headers = headers
+            for name in abi.TRACE_ARRAYS:
+                a = np.zeros(max_records * nlefs, dtype=np.uint64)
+                arrays[name] = a
+                setattr(tr, name, abi.ptr64(a))
+        all_headers = (abi.TraceHeader * max(1, max_epochs))()
+        if max_epochs:
+            tr.max_epochs = max_epochs
+            tr.all_headers = all_headers
+        st = abi.CellStats()
+        band_ptr = band.ctypes.data if isinstance(band, np.ndarray) else band
+        _check(self.lib.mgpu_trace_cell(self.h, chrom_id, seed, target, target_epochs, nlefs,
+                                        band_ptr, C.byref(st), C.byref(tr)), "mgpu_trace_cell")
+        return st, headers, arrays, all_headers, tr.num_epochs_recorded
+
+    def set_stream(self, stream_handle):
+        """Launch on a caller's cudaStream_t (an int handle, e.g. torch's stream.cuda_stream)."""
+        _check(self.lib.mgpu_set_stream(self.h, C.c_void_p(stream_handle)), "mgpu_set_stream")
+
+    def last_kernel_ms(self):
+        ms = C.c_double()
+        _check(self.lib.mgpu_last_kernel_ms(self.h, C.byref(ms)), "mgpu_last_kernel_ms")
+        return ms.value
+
+    def run_phase(self, chrom_id, phase, io):
+        return self.lib.mgpu_run_phase(self.h, chrom_id, phase, C.byref(io))

@@ -1,0 +1,85 @@
+"""Seeded synthetic genomes for the workloads the engine is measured and checked on.
+
+The reference benchmarks on no public dataset (its integration test's GRCh38 inputs are
+not shipped), so every workload is generated here from a fixed seed with the shapes of the
+parity and genome-scale workloads:
+
+* ``parity_10mbp``: one 10 Mbp chromosome, 5 kb bins, 3 Mbp band (600 x 2000 uint32 band),
+  100 barriers at uniform positions with +/- strands (p = 0.5), stp 0.7/0.7 (occupancy 0.5),
+  20 LEFs/Mbp, 200 kb lifetime, 2.5 kb/epoch speeds with 5 % std, 64 cells, contact density 1,
+  probability normalisation factor 5000 (keeps the stps as stated).
+* ``genome_24chr``: 24 chromosomes with lengths uniform in [50, 250] Mbp, one barrier per
+  50 kb on average at uniform positions, random strands, occupancy ~ Beta(8, 2) written to
+  the BED score, 20 LEFs/Mbp, 200 kb lifetime, default speeds (0.8 x bin), 512 cells each.
+
+Barriers are produced as BED records [p, p + 1) (so the reference's midpoint rule
+(start + end + 1) / 2 of genome.cpp:199 puts the barrier at p + 1) in IITree order (sorted by
+start, distinct positions), then converted with mgpu_barrier_from_bed.
+"""
+
+import numpy as np
+
+from . import engine
+
+
+def _distinct_positions(rng, lo, hi, k):
+    pos = np.unique(rng.integers(lo, hi, size=k, dtype=np.int64))
+    while len(pos) < k:
+        extra = rng.integers(lo, hi, size=k - len(pos), dtype=np.int64)
+        pos = np.unique(np.concatenate([pos, extra]))
+    return np.sort(pos[:k])
+
+
+def bed_records(rng, length, nbarriers, occupancy=None):
+    """BED6-like records (start, end, strand, score) of barriers on [0, length)."""
+    starts = _distinct_positions(rng, 0, length - 1, nbarriers)
+    strands = np.where(rng.random(nbarriers) < 0.5, "+", "-")
+    scores = occupancy if occupancy is not None else np.zeros(nbarriers)
+    return [(int(s), int(s) + 1, str(st), float(sc)) for s, st, sc in zip(starts, strands, scores)]
+
+
+def parity_config(**overrides):
+    """Transformed Config of the 10 Mbp parity workload."""
+    cfg = engine.config_defaults(
+        bin_size=5000, diagonal_width=3_000_000, rev_extrusion_speed=2500, fwd_extrusion_speed=2500,
+        rev_speed_set=1, fwd_speed_set=1, rev_extrusion_speed_std=0.05, fwd_extrusion_speed_std=0.05,
+        number_of_lefs_per_mbp=20.0, avg_lef_processivity=200_000, barrier_occupied_stp=0.7,
+        barrier_not_occupied_stp=0.7, probability_normalization_factor=5000, num_cells=64,
+        seed=20231203, target_contact_density=1.0)
+    for k, v in overrides.items():
+        setattr(cfg, k, v)
+    return engine.config_transform(cfg)
+
+
+def parity_10mbp(seed=7, **overrides):
+    cfg = parity_config(**overrides)
+    rng = np.random.default_rng(seed)
+    chrom = engine.Chromosome("chrS", 10_000_000)
+    recs = bed_records(rng, chrom.size, 100)
+    bars = engine.barriers_from_bed(chrom, recs, cfg.barrier_occupied_stp, cfg.barrier_not_occupied_stp)
+    return cfg, [(chrom, bars)]
+
+
+def genome_config(**overrides):
+    """Transformed Config of the genome-scale workload (defaults except lifetime, 512 cells)."""
+    cfg = engine.config_defaults(bin_size=5000, diagonal_width=3_000_000, number_of_lefs_per_mbp=20.0,
+                                 avg_lef_processivity=200_000, num_cells=512, seed=20231203,
+                                 target_contact_density=1.0)
+    for k, v in overrides.items():
+        setattr(cfg, k, v)
+    return engine.config_transform(cfg)
+
+
+def genome_24chr(seed=11, nchroms=24, min_len=50_000_000, max_len=250_000_000, **overrides):
+    cfg = genome_config(**overrides)
+    rng = np.random.default_rng(seed)
+    lengths = rng.integers(min_len, max_len + 1, size=nchroms)
+    out = []
+    for k, L in enumerate(lengths):
+        chrom = engine.Chromosome(f"chr{k + 1}", int(L))
+        nb = int(round(L / 50_000))
+        occ = rng.beta(8.0, 2.0, size=nb)
+        recs = bed_records(rng, int(L), nb, occ)
+        bars = engine.barriers_from_bed(chrom, recs, cfg.barrier_occupied_stp, cfg.barrier_not_occupied_stp)
+        out.append((chrom, bars))
+    return cfg, out

@@ -1,0 +1,59 @@
+"""Host driver of a genome-wide run: the task fan-out of Simulation::run_simulate
+(src/libmodle/cpu/scheduler_simulate.cpp:110-166) over the engine's batched call.
+
+Per chromosome: the number of LEFs (simulation.cpp:1253-1257), the per-cell contact targets
+(scheduler_simulate.cpp:129-153), the per-cell seeds (genome.cpp:317-335), then one
+``mgpu_simulate_cells`` call for all of its cells (one launch per chromosome).  Chromosomes
+without barriers are skipped unless ``simulate_chromosomes_wo_barriers`` is set
+(scheduler_simulate.cpp:114-121).
+"""
+
+import numpy as np
+
+from . import engine
+
+
+class ChromResult:
+    def __init__(self, chrom, nlefs, band, missed, stats):
+        self.chrom = chrom
+        self.nlefs = nlefs
+        self.band = band
+        self.missed = missed
+        self.stats = stats
+
+    @property
+    def lef_epochs(self):
+        return int(sum(s.lef_epochs for s in self.stats))
+
+    @property
+    def contacts(self):
+        return int(sum(s.contacts for s in self.stats))
+
+
+def prepare_chrom(eng, cfg, chrom, barriers, ncells):
+    """Upload one chromosome and compute its task list; returns a dict of launch inputs."""
+    size = chrom.simulated_size
+    nlefs = engine.num_lefs(cfg, size)
+    targets, target_epochs = engine.task_targets(cfg, size, nlefs, ncells)
+    seeds = np.array([engine.cell_seed(chrom.name, chrom.size, cfg.seed, i) for i in range(ncells)],
+                     dtype=np.uint64)
+    cid = eng.upload_chrom(chrom, barriers)
+    nrows, ncols = engine.band_shape(cfg, size)
+    return dict(chrom=chrom, cid=cid, nlefs=nlefs, targets=targets, target_epochs=target_epochs,
+                seeds=seeds, nrows=nrows, ncols=ncols)
+
+
+def simulate_genome(cfg, genome, ncells=None, device=0, simulate_wo_barriers=False):
+    """Run every cell of every chromosome; returns a list of ChromResult."""
+    ncells = int(cfg.num_cells if ncells is None else ncells)
+    out = []
+    with engine.Engine(cfg, device) as eng:
+        for chrom, barriers in genome:
+            if not barriers and not simulate_wo_barriers:
+                continue
+            t = prepare_chrom(eng, cfg, chrom, barriers, ncells)
+            band = np.zeros(t["nrows"] * t["ncols"], dtype=np.uint32)
+            missed, stats = eng.simulate_cells(t["cid"], t["seeds"], t["targets"], t["target_epochs"],
+                                               t["nlefs"], band)
+            out.append(ChromResult(chrom, t["nlefs"], band, missed, stats))
+    return out
