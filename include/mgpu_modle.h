@@ -224,6 +224,13 @@ int mgpu_sync(mgpu_ctx* ctx);
 int mgpu_set_stream(mgpu_ctx* ctx, void* cuda_stream);
 int mgpu_last_kernel_ms(mgpu_ctx* ctx, double* ms);
 
+/* Test and tuning switches (no counterpart in the reference).  flags: bit 0 ranks, bit 1
+ * move adjustment, bit 2 collision processing, bit 3 contact sampling use the exact serial
+ * restatement instead of the warp-parallel form (results are identical either way);
+ * smem_budget caps the shared memory one cell may use (0 = device limit), placing the
+ * remaining per-LEF arrays in global scratch. */
+int mgpu_set_debug_flags(mgpu_ctx* ctx, uint32_t flags, uint64_t smem_budget);
+
 /* Upload one chromosome and its barriers (sorted with mgpu_sort_barriers order); returns a
  * handle in *chrom_id.  Barriers are shared by every cell of the chromosome. */
 int mgpu_upload_chrom(mgpu_ctx* ctx, const mgpu_chrom* chrom, const mgpu_barrier* barriers,

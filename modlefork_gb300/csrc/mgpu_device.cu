@@ -1,26 +1,36 @@
 // mgpu_device.cu - sm_103a kernels of the loop-extrusion epoch engine.
 //
 // One warp simulates one cell (Simulation::simulate_one_cell, src/libmodle/cpu/
-// simulation.cpp:1056-1152).  The cell's whole state lives in shared memory as 32-bit
-// structure-of-arrays; the barrier track and its integer thresholds are read-only in global
-// memory and shared by every cell of the chromosome.  The kernel is persistent: each warp
-// pulls cell indices from a global work counter until the batch is drained.
+// simulation.cpp:1056-1152).  The cell's state is structure-of-arrays of 32-bit words; the
+// host plans which per-LEF arrays fit in the cell's shared memory and places the rest in a
+// per-cell global scratch slot (large chromosomes).  The barrier track and its integer
+// thresholds are read-only in global memory and shared by every cell of the chromosome.
+// The kernel is persistent: each warp pulls cell indices from a global work counter.
 //
 // Draw order.  Every random number of the reference comes from one sequential
 // Xoshiro256++ stream per cell, consumed in a data-dependent order.  The warp keeps a ring of
-// pre-generated draws in shared memory: all 32 lanes generate RNG_S consecutive draws each
-// per refill, and then advance their private state by 31 * RNG_S steps with a GF(2) jump
-// table (the state transition of xoshiro is linear), so the ring always holds the exact
-// stream.  Phases whose items take one draw each (binding, barrier steps, moves, release)
-// give lane k the draw at offset popc(ballot & lanemask_lt); the rare item that needs more
-// draws (a ziggurat wedge or tail, a bucket rejection) is finished by lane 0 from its exact
-// offset and the warp resumes after it.  Sequential sweeps (collision detection, chains of
-// secondary collisions, the exact split_sort) run on lane 0 and read draws serially.
+// pre-generated draws in shared memory: all 32 lanes generate RNG_S consecutive draws each per
+// refill and then advance their private state by 31 * RNG_S steps with a GF(2) jump table (the
+// state transition of xoshiro is linear), so the ring always holds the exact stream.
+//
+// Every step of the epoch runs warp-parallel with the exact draw order:
+//  * steps whose items take one draw each (binding, barrier steps, moves, release, LEF-BAR
+//    and LEF-LEF trials) give lane k the draw at offset popc(ballot & lanemask_lt);
+//  * items that may take more draws (ziggurat wedges and tails, rejected contact attempts,
+//    failed bypass trials in a chain of secondary collisions) are evaluated speculatively at
+//    the offsets they would have if every earlier item took its usual count; the first item
+//    that deviates is resolved exactly and the warp resumes after it;
+//  * sequential sweeps are replaced by closed forms: rank_lefs by a merge of the units bound
+//    this epoch into the still-sorted order of the others, adjust_moves by segmented min/max
+//    scans, the LEF-BAR and primary LEF-LEF sweeps by binary searches over the ranked
+//    positions.
+// Where a closed form's precondition does not hold (full ties in the ranking, a chain that
+// reaches a chromosome end, unsorted caller input), the step falls back to a line-by-line
+// serial restatement run by lane 0, so results never depend on the fast path.
 //
 // Floating point.  The file is compiled with --fmad=false so every double multiply and add
 // is rounded separately, like the reference's x86-64 build; bernoulli and
-// generate_canonical comparisons are replaced by exact integer thresholds computed on the
-// host.
+// generate_canonical comparisons are exact integer thresholds computed on the host.
 
 #include <cuda_runtime.h>
 
@@ -34,6 +44,7 @@
 namespace mgpu {
 
 #define MGPU_ITER_LIMIT 100000000ull
+#define FULL 0xFFFFFFFFu
 
 __device__ __forceinline__ u64 rotl64(u64 x, int k) { return (x << k) | (x >> (64 - k)); }
 
@@ -55,7 +66,21 @@ __device__ __forceinline__ unsigned lanemask_lt() {
   return m;
 }
 
+__device__ __forceinline__ u32 ln() { return threadIdx.x & 31u; }
+
 __device__ __forceinline__ u64 pos64(u32 v) { return v == UNBOUND ? ~0ull : (u64)v; }
+
+// exclusive prefix sum over the warp; *total receives the sum of all lanes
+__device__ __forceinline__ u32 warp_excl_scan(u32 v, u32* total) {
+  u32 x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const u32 y = __shfl_up_sync(FULL, x, d);
+    if ((int)ln() >= d) x += y;
+  }
+  if (total) *total = __shfl_sync(FULL, x, 31);
+  return x - v;
+}
 
 // Cell scalars (warp-uniform, kept in shared memory so lane 0's serial code can update them).
 struct Scalars {
@@ -64,24 +89,25 @@ struct Scalars {
   u32 lanes_stale; // lanes must re-derive their states from canon before the next refill
   u32 status;
   u64 epoch, num_burnin_epochs, num_active, num_contacts;
-  u32 burnin_completed, pad0;
+  u32 burnin_completed, flag;
   u64 missed, lef_epochs, sort_fallbacks;
   u64 n5, n3;
   u32 hist_size, hist_head;
-  u64 records;
+  u64 bc0, bc1, bc2;  // broadcast slots for lane 0 results
 };
+static_assert(sizeof(Scalars) <= CELL_HEADER_BYTES, "scalars do not fit the cell header");
 
+// Pointers of one cell (lives in shared memory; identical for every lane).
 struct Cell {
   Scalars* sc;
   u64* ring;
-  u32 *rev, *fwd, *bep, *rr, *fr, *rm, *fm, *rc, *fc, *tmp;
+  u32 *rev, *fwd, *rr, *fr, *rm, *fm, *rc, *fc, *sr, *sf, *tmp, *bep;
   u32* bst;
   double *hcfx, *havg;
   const DevBarrier* bar;
   u32 nb;
+  u32 nl;
   const ulonglong2* jt;
-  int lane;
-  u64 s[4];
   u32* band;
 };
 
@@ -106,28 +132,30 @@ __device__ __forceinline__ void xo_jump(u64* s, const ulonglong2* jt) {
   s[3] = n3;
 }
 
-// Collective: append RNG_BLOCK draws to the ring.
-__device__ __noinline__ void rng_refill(Cell& c) {
+// Collective: append RNG_BLOCK draws to the ring.  s is this lane's private stream state.
+__device__ __noinline__ void rng_refill(Cell& c, u64* s) {
   Scalars* sc = c.sc;
+  const u32 lane = ln();
   if (sc->lanes_stale) {
-    for (int k = 0; k < 4; ++k) c.s[k] = sc->canon[k];
-    for (int t = 0; t < c.lane * RNG_S; ++t) xo_next(c.s);
+    for (int k = 0; k < 4; ++k) s[k] = sc->canon[k];
+    for (u32 t = 0; t < lane * RNG_S; ++t) xo_next(s);
   }
   const u64 g = sc->gpos;
-  for (int k = 0; k < RNG_S; ++k) c.ring[(g + (u64)c.lane * RNG_S + k) & (RING - 1)] = xo_next(c.s);
-  xo_jump(c.s, c.jt);
+#pragma unroll 4
+  for (int k = 0; k < RNG_S; ++k) c.ring[(g + (u64)lane * RNG_S + k) & (RING - 1)] = xo_next(s);
+  xo_jump(s, c.jt);
   __syncwarp();
-  if (c.lane == 0) {
+  if (lane == 0) {
     sc->gpos = g + RNG_BLOCK;
-    for (int k = 0; k < 4; ++k) sc->canon[k] = c.s[k];
+    for (int k = 0; k < 4; ++k) sc->canon[k] = s[k];
     sc->lanes_stale = 0;
   }
   __syncwarp();
 }
 
 // Collective: make at least n (<= RNG_BLOCK) unconsumed draws available.
-__device__ __forceinline__ void rng_ensure(Cell& c, u32 n) {
-  while (c.sc->gpos - c.sc->rpos < n) rng_refill(c);
+__device__ __forceinline__ void rng_ensure(Cell& c, u64* s, u32 n) {
+  while (c.sc->gpos - c.sc->rpos < n) rng_refill(c, s);
 }
 
 __device__ __forceinline__ u64 ring_at(const Cell& c, u64 k) { return c.ring[k & (RING - 1)]; }
@@ -146,13 +174,14 @@ __device__ u64 rng_serial(Cell& c) {
   return v;
 }
 
+__device__ __forceinline__ void set_status(Cell& c, u32 st) {
+  if (c.sc->status == DEV_OK) c.sc->status = st;
+}
+
 // ---------------------------------------------------------------------------------------
 // Serial distributions (lane 0).  Boost.Random 1.79 semantics, see the oracle for the
 // line-by-line restatement; thresholds replace bernoulli / canonical comparisons.
 // ---------------------------------------------------------------------------------------
-__device__ __forceinline__ void set_status(Cell& c, u32 st) {
-  if (c.sc->status == DEV_OK) c.sc->status = st;
-}
 
 __device__ u64 s_uniform_int(Cell& c, u64 a, u64 b) {
   const u64 range = b - a;
@@ -434,222 +463,65 @@ __device__ double s_gev(Cell& c, const KParams& P) {
   return P.gev_mu + (P.gev_sigma * (1.0 - pow(-log(u), P.gev_xi))) / P.gev_xi;
 }
 
-// rank_lefs (simulation.cpp:402-487); lane 0
-__device__ void rank_lefs_serial(Cell& c, u32 n, bool partially_sorted, bool init) {
-  if (init) {
-    for (u32 i = 0; i < n; ++i) {
-      c.rr[i] = i;
-      c.fr[i] = i;
-    }
-  }
-  const KeyCmp rcmp{c.rev}, fcmp{c.fwd};
+
+// ---------------------------------------------------------------------------------------
+// Serial restatements (lane 0): the exact fallbacks of the warp-parallel steps
+// ---------------------------------------------------------------------------------------
+
+// rank_lefs for one direction (simulation.cpp:402-487): split_sort (or pdq_sort at epoch 0)
+// by position, then runs of equal positions insertion-sorted by binding epoch (ascending
+// for rev units, descending for fwd units).
+__device__ void rank_dir_serial(Cell& c, u32 dir, u32 n, bool partially_sorted) {
+  u32* R = dir ? c.fr : c.rr;
+  const u32* pos = dir ? c.fwd : c.rev;
+  const KeyCmp cmp{pos};
   if (partially_sorted) {
-    split_sort(c.rr, n, c.tmp, rcmp);
-    split_sort(c.fr, n, c.tmp, fcmp);
+    split_sort(R, n, c.tmp, cmp);
   } else {
-    pdq_sort(c.rr, 0, n, rcmp);
-    pdq_sort(c.fr, 0, n, fcmp);
+    pdq_sort(R, 0, n, cmp);
   }
   for (u32 i = 1; i < n; ++i) {
-    if (c.rev[c.rr[i - 1]] == c.rev[c.rr[i]]) {
+    if (pos[R[i - 1]] == pos[R[i]]) {
       const u32 begin = i - 1;
       for (; i < n; ++i) {
-        if (c.rev[c.rr[i - 1]] != c.rev[c.rr[i]]) break;
+        if (pos[R[i - 1]] != pos[R[i]]) break;
       }
-      ins_sort(c.rr, begin, i, KeyCmp{c.bep});
-    }
-  }
-  for (u32 i = 1; i < n; ++i) {
-    if (c.fwd[c.fr[i - 1]] == c.fwd[c.fr[i]]) {
-      const u32 begin = i - 1;
-      for (; i < n; ++i) {
-        if (c.fwd[c.fr[i - 1]] != c.fwd[c.fr[i]]) break;
-      }
-      ins_sort(c.fr, begin, i, KeyCmpRev{c.bep});
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------------------
-// Epoch steps
-// ---------------------------------------------------------------------------------------
-
-// ExtrusionBarriers::init_states (extrusion_barriers.cpp:220-231): warp-parallel.
-__device__ void barriers_init(Cell& c) {
-  for (u32 base = 0; base < c.nb; base += 32) {
-    rng_ensure(c, 32);
-    const u32 i = base + c.lane;
-    const bool need = i < c.nb && (c.bar[i].flags & BF_OCC_DRAWS);
-    const unsigned m = __ballot_sync(0xFFFFFFFFu, need);
-    const u32 off = __popc(m & lanemask_lt());
-    bool occ = false;
-    if (need) occ = ring_at(c, c.sc->rpos + off) <= c.bar[i].t_occ;
-    const unsigned om = __ballot_sync(0xFFFFFFFFu, occ);
-    __syncwarp();
-    if (c.lane == 0) {
-      c.bst[base >> 5] = om;
-      c.sc->rpos += __popc(m);
-    }
-    __syncwarp();
-  }
-}
-
-// ExtrusionBarriers::next_state (extrusion_barriers.cpp:145-161): one draw per barrier.
-__device__ void barriers_next(Cell& c) {
-  for (u32 base = 0; base < c.nb; base += 32) {
-    rng_ensure(c, 32);
-    const u32 i = base + c.lane;
-    const bool valid = i < c.nb;
-    bool st = (c.bst[base >> 5] >> c.lane) & 1u;
-    if (valid) {
-      const u64 u = ring_at(c, c.sc->rpos + c.lane);
-      const u32 f = c.bar[i].flags;
-      if (!st) {
-        st = !(f & BF_INA_NEVER) && u >= c.bar[i].t_ina;
+      if (dir) {
+        ins_sort(R, begin, i, KeyCmpRev{c.bep});
       } else {
-        st = !(!(f & BF_ACT_NEVER) && u >= c.bar[i].t_act);
+        ins_sort(R, begin, i, KeyCmp{c.bep});
       }
     }
-    const unsigned nm = __ballot_sync(0xFFFFFFFFu, valid && st);
-    __syncwarp();
-    if (c.lane == 0) {
-      c.bst[base >> 5] = nm;
-      c.sc->rpos += min(32u, c.nb - base);
-    }
-    __syncwarp();
   }
 }
 
-__device__ __forceinline__ bool bar_active(const Cell& c, u32 i) { return (c.bst[i >> 5] >> (i & 31)) & 1u; }
-
-// select_lefs_to_bind + bind_lefs (simulation_impl.hpp:28-89): warp-parallel, one
-// uniform_int draw per selected LEF in index order.  Selection: mode 0 = unbound LEFs (the
-// epoch loop), 1 = nonzero entries of mask, 2 = every LEF (an empty mask in the reference).
-__device__ __forceinline__ bool bind_selected(const Cell& c, u32 i, int mode, const u64* mask) {
-  return mode == 0 ? c.bep[i] == UNBOUND : (mode == 1 ? mask[i] != 0 : true);
-}
-
-__device__ void bind_lefs(Cell& c, const KParams& P, u32 n, u32 epoch, int mode, const u64* mask) {
-  u32 i0 = 0;
-  while (i0 < n) {
-    rng_ensure(c, 32);
-    const u32 i = i0 + c.lane;
-    const bool need = i < n && bind_selected(c, i, mode, mask);
-    const unsigned m = __ballot_sync(0xFFFFFFFFu, need);
-    const u32 off = __popc(m & lanemask_lt());
-    u64 r = 0;
-    bool ok = true;
-    if (need) {
-      r = ring_at(c, c.sc->rpos + off) / P.pos_bucket;
-      ok = r <= P.pos_range;
-    }
-    const unsigned bad = __ballot_sync(0xFFFFFFFFu, need && !ok);
-    const u32 f = bad ? (u32)(__ffs(bad) - 1) : 32u;
-    if (need && c.lane < f) {
-      const u32 pos = (u32)(P.start + r);
-      c.rev[i] = pos;
-      c.fwd[i] = pos;
-      c.bep[i] = epoch;
-    }
-    __syncwarp();
-    if (c.lane == 0) {
-      c.sc->rpos += __popc(m & (f == 32 ? 0xFFFFFFFFu : ((1u << f) - 1)));
-      if (f < 32) {  // finish this chunk serially from the rejecting LEF
-        for (u32 k = i0 + f; k < min(i0 + 32, n); ++k) {
-          const bool nk = bind_selected(c, k, mode, mask);
-          if (!nk) continue;
-          const u64 pos = s_uniform_int(c, P.start, (u64)P.end - 1);
-          c.rev[k] = (u32)pos;
-          c.fwd[k] = (u32)pos;
-          c.bep[k] = epoch;
-        }
-      }
-    }
-    __syncwarp();
-    i0 += 32;
-  }
-}
-
-// generate_moves_helper (simulation.cpp:264-290): warp-parallel speculation on the ziggurat
-// fast path; the first item that needs more draws is finished serially by lane 0.
-__device__ void gen_moves_dir(Cell& c, u32* mv, u32 n, double mean, double sd, u64 move_int) {
-  if (sd == 0.0) {
-    for (u32 i = c.lane; i < n; i += 32) mv[i] = c.bep[i] == UNBOUND ? 0u : (u32)move_int;
-    __syncwarp();
-    return;
-  }
-  u32 i0 = 0;
-  while (i0 < n) {
-    rng_ensure(c, 64);
-    const u32 i = i0 + c.lane;
-    const bool need = i < n && c.bep[i] != UNBOUND;
-    const unsigned m = __ballot_sync(0xFFFFFFFFu, need);
-    const u32 off = __popc(m & lanemask_lt());
-    double z = 0;
-    bool ok = true;
-    if (need) ok = normal_fast(ring_at(c, c.sc->rpos + off), z);
-    const unsigned bad = __ballot_sync(0xFFFFFFFFu, need && !ok);
-    const u32 f = bad ? (u32)(__ffs(bad) - 1) : 32u;
-    if (i < n && c.lane < f) {
-      if (need) {
-        const double v = round(fmax(0.0, z * sd + mean));
-        if (v > 4294967295.0) set_status(c, DEV_ERR_MOVE_RANGE);
-        mv[i] = (u32)(u64)v;
-      } else {
-        mv[i] = 0;
-      }
-    }
-    __syncwarp();
-    if (c.lane == 0) {
-      c.sc->rpos += __popc(m & (f == 32 ? 0xFFFFFFFFu : ((1u << f) - 1)));
-      if (f < 32) {
-        const double zz = s_unit_normal(c);
-        const double v = round(fmax(0.0, zz * sd + mean));
-        if (v > 4294967295.0) set_status(c, DEV_ERR_MOVE_RANGE);
-        mv[i0 + f] = (u32)(u64)v;
-      }
-    }
-    __syncwarp();
-    i0 += (f == 32) ? 32 : f + 1;
-  }
-}
-
-// adjust_moves_of_consecutive_extr_units (simulation.cpp:343-399); lane 0
-__device__ void adjust_moves_serial(Cell& c, const KParams& P, u32 n) {
+// adjust_moves_of_consecutive_extr_units (simulation.cpp:343-399), one direction; lane 0
+__device__ void adjust_dir_serial(Cell& c, const KParams& P, u32 dir, u32 n) {
   if (n == 0) return;
   const u64 start = P.start, end = P.end;
-  for (u32 i = n - 1; i > 0; --i) {
-    const u32 i1 = c.rr[i - 1], i2 = c.rr[i];
-    if (c.bep[i1] != UNBOUND && c.bep[i2] != UNBOUND) {
-      const u64 r1 = pos64(c.rev[i1]), r2 = pos64(c.rev[i2]);
-      const u64 m1 = c.rm[i1], m2 = c.rm[i2];
-      if (r1 <= start + m1 || r2 <= start + m2) continue;
-      const u64 pos1 = r1 - m1, pos2 = r2 - m2;
-      if (pos2 <= pos1) c.rm[i1] = (u32)(m1 + (pos1 - pos2) + 1);
+  if (dir == 0) {
+    for (u32 i = n - 1; i > 0; --i) {
+      const u32 i1 = c.rr[i - 1], i2 = c.rr[i];
+      if (c.bep[i1] != UNBOUND && c.bep[i2] != UNBOUND) {
+        const u64 r1 = pos64(c.rev[i1]), r2 = pos64(c.rev[i2]);
+        const u64 m1 = c.rm[i1], m2 = c.rm[i2];
+        if (r1 <= start + m1 || r2 <= start + m2) continue;
+        const u64 pos1 = r1 - m1, pos2 = r2 - m2;
+        if (pos2 <= pos1) c.rm[i1] = (u32)(m1 + (pos1 - pos2) + 1);
+      }
+    }
+  } else {
+    for (u32 i = 1; i < n; ++i) {
+      const u32 i1 = c.fr[i - 1], i2 = c.fr[i];
+      if (c.bep[i1] != UNBOUND && c.bep[i2] != UNBOUND) {
+        const u64 f1 = pos64(c.fwd[i1]), f2 = pos64(c.fwd[i2]);
+        const u64 m1 = c.fm[i1], m2 = c.fm[i2];
+        if (f1 + m1 > end - 1 || f2 + m2 > end - 1) continue;
+        const u64 pos1 = f1 + m1, pos2 = f2 + m2;
+        if (pos1 >= pos2) c.fm[i2] = (u32)(m2 + (pos1 - pos2) + 1);
+      }
     }
   }
-  for (u32 i = 1; i < n; ++i) {
-    const u32 i1 = c.fr[i - 1], i2 = c.fr[i];
-    if (c.bep[i1] != UNBOUND && c.bep[i2] != UNBOUND) {
-      const u64 f1 = pos64(c.fwd[i1]), f2 = pos64(c.fwd[i2]);
-      const u64 m1 = c.fm[i1], m2 = c.fm[i2];
-      if (f1 + m1 > end - 1 || f2 + m2 > end - 1) continue;
-      const u64 pos1 = f1 + m1, pos2 = f2 + m2;
-      if (pos1 >= pos2) c.fm[i2] = (u32)(m2 + (pos1 - pos2) + 1);
-    }
-  }
-}
-
-// clamp_moves (simulation.cpp:325-340): warp-parallel
-__device__ void clamp_moves(Cell& c, const KParams& P, u32 n) {
-  for (u32 i = c.lane; i < n; i += 32) {
-    if (c.bep[i] == UNBOUND) continue;
-    const u64 rmv = min((u64)c.rm[i], pos64(c.rev[i]) - P.start);
-    const u64 fmv = min((u64)c.fm[i], (u64)P.end - pos64(c.fwd[i]) - 1);
-    c.rm[i] = (u32)rmv;
-    c.fm[i] = (u32)fmv;
-  }
-  __syncwarp();
 }
 
 // compute_lef_lef_collision_pos (simulation.cpp:514-542)
@@ -667,7 +539,9 @@ __device__ __forceinline__ void lef_lef_collision_pos(u64 rev_pos, u64 fwd_pos, 
   }
 }
 
-// detect_units_at_chrom_boundaries (simulation_detect_collisions.cpp:30-125); lane 0
+
+// detect_units_at_chrom_boundaries (simulation_detect_collisions.cpp:30-125); lane 0.  The
+// loops stop at the first unit that is neither at nor about to reach a chromosome end.
 __device__ void detect_boundaries_serial(Cell& c, const KParams& P, u32 n, u64& n5, u64& n3) {
   n5 = 0;
   n3 = 0;
@@ -720,6 +594,8 @@ __device__ void detect_boundaries_serial(Cell& c, const KParams& P, u32 n, u64& 
     }
   }
 }
+
+__device__ __forceinline__ bool bar_active(const Cell& c, u32 i) { return (c.bst[i >> 5] >> (i & 31)) & 1u; }
 
 // detect_lef_bar_collisions (simulation_detect_collisions.cpp:128-252); lane 0
 __device__ void detect_lef_bar_serial(Cell& c, const KParams& P, u32 n, u64 n5, u64 n3) {
@@ -778,6 +654,30 @@ __device__ __forceinline__ u64 barrier_pos_checked(Cell& c, u32 idx) {
   return c.bar[idx].pos;
 }
 
+// The collision words of one tested primary pair (simulation_detect_collisions.cpp:344-399).
+__device__ __forceinline__ void primary_pair_update(Cell& c, u32 rev_idx, u32 fwd_idx, u64 rev_pos,
+                                                    u64 fwd_pos, u64 rmv, u64 fmv) {
+  u64 cpr, cpf;
+  lef_lef_collision_pos(rev_pos, fwd_pos, rmv, fmv, cpr, cpf);
+  const u32 rcol = c.rc[rev_idx], fcol = c.fc[fwd_idx];
+  if (!cw_occurred(rcol) && !cw_occurred(fcol)) {
+    c.rc[rev_idx] = cw_make(fwd_idx, EV_COLLISION | EV_PRIMARY);
+    c.fc[fwd_idx] = cw_make(rev_idx, EV_COLLISION | EV_PRIMARY);
+  } else if (cw_occurred(rcol) && !cw_occurred(fcol)) {
+    const u64 bpos = barrier_pos_checked(c, cw_idx(rcol));
+    if (cpf > bpos) {
+      c.rc[rev_idx] = cw_make(fwd_idx, EV_COLLISION | EV_PRIMARY);
+      c.fc[fwd_idx] = cw_make(rev_idx, EV_COLLISION | EV_PRIMARY);
+    } else {
+      c.fc[fwd_idx] = cw_make(rev_idx, EV_COLLISION | EV_PRIMARY);
+    }
+  } else if (!cw_occurred(rcol) && cw_occurred(fcol)) {
+    const u64 bpos = barrier_pos_checked(c, cw_idx(fcol));
+    c.rc[rev_idx] = cw_make(fwd_idx, EV_COLLISION | EV_PRIMARY);
+    if (cpr < bpos) c.fc[fwd_idx] = cw_make(rev_idx, EV_COLLISION | EV_PRIMARY);
+  }
+}
+
 // detect_primary_lef_lef_collisions (simulation_detect_collisions.cpp:255-401); lane 0
 __device__ void detect_primary_serial(Cell& c, const KParams& P, u32 n, u64 n5, u64 n3) {
   if (n5 == n || n3 == n) return;
@@ -804,70 +704,10 @@ __device__ void detect_primary_serial(Cell& c, const KParams& P, u32 n, u64 n5, 
     const u64 delta = rev_pos - fwd_pos;
     const u64 rmv = c.rm[rev_idx], fmv = c.fm[fwd_idx];
     if (delta > 0 && delta < rmv + fmv && s_trial(c, P.lef_lef)) {
-      u64 cpr, cpf;
-      lef_lef_collision_pos(rev_pos, fwd_pos, rmv, fmv, cpr, cpf);
-      const u32 rcol = c.rc[rev_idx], fcol = c.fc[fwd_idx];
-      if (!cw_occurred(rcol) && !cw_occurred(fcol)) {
-        c.rc[rev_idx] = cw_make(fwd_idx, EV_COLLISION | EV_PRIMARY);
-        c.fc[fwd_idx] = cw_make(rev_idx, EV_COLLISION | EV_PRIMARY);
-      } else if (cw_occurred(rcol) && !cw_occurred(fcol)) {
-        const u64 bpos = barrier_pos_checked(c, cw_idx(rcol));
-        if (cpf > bpos) {
-          c.rc[rev_idx] = cw_make(fwd_idx, EV_COLLISION | EV_PRIMARY);
-          c.fc[fwd_idx] = cw_make(rev_idx, EV_COLLISION | EV_PRIMARY);
-        } else {
-          c.fc[fwd_idx] = cw_make(rev_idx, EV_COLLISION | EV_PRIMARY);
-        }
-      } else if (!cw_occurred(rcol) && cw_occurred(fcol)) {
-        const u64 bpos = barrier_pos_checked(c, cw_idx(fcol));
-        c.rc[rev_idx] = cw_make(fwd_idx, EV_COLLISION | EV_PRIMARY);
-        if (cpr < bpos) c.fc[fwd_idx] = cw_make(rev_idx, EV_COLLISION | EV_PRIMARY);
-      }
+      primary_pair_update(c, rev_idx, fwd_idx, rev_pos, fwd_pos, rmv, fmv);
     }
   }
   set_status(c, DEV_ERR_ITER_LIMIT);
-}
-
-// correct_moves_for_lef_bar_collisions (simulation_correct_moves.cpp:20-51): warp-parallel
-__device__ void correct_lef_bar(Cell& c, u32 n) {
-  for (u32 i = c.lane; i < n; i += 32) {
-    const u32 r = c.rc[i], f = c.fc[i];
-    if (cw_occurred_as(r, EV_LEF_BAR)) c.rm[i] = (u32)(pos64(c.rev[i]) - c.bar[cw_idx(r)].pos - 1);
-    if (cw_occurred_as(f, EV_LEF_BAR)) c.fm[i] = (u32)(c.bar[cw_idx(f)].pos - pos64(c.fwd[i]) - 1);
-  }
-  __syncwarp();
-}
-
-// correct_moves_for_primary_lef_lef_collisions (simulation_correct_moves.cpp:54-122):
-// the pairs it visits are disjoint, so both passes are warp-parallel.
-__device__ void correct_primary(Cell& c, u32 n) {
-  for (u32 k = c.lane; k < n; k += 32) {
-    const u32 rev_idx = c.rr[k];
-    const u32 r = c.rc[rev_idx];
-    if (!cw_occurred_as(r, EV_PRIMARY)) continue;
-    const u32 fwd_idx = cw_idx(r);
-    const u32 f = c.fc[fwd_idx];
-    if (cw_occurred_as(f, EV_PRIMARY)) {
-      const u64 rp = pos64(c.rev[rev_idx]), fp = pos64(c.fwd[fwd_idx]);
-      u64 p1, p2;
-      lef_lef_collision_pos(rp, fp, c.rm[rev_idx], c.fm[fwd_idx], p1, p2);
-      c.rm[rev_idx] = (u32)(rp - p1);
-      c.fm[fwd_idx] = (u32)(p2 - fp);
-    } else if (cw_occurred_as(f, EV_LEF_BAR)) {
-      c.rm[rev_idx] = (u32)(pos64(c.rev[rev_idx]) - (pos64(c.fwd[fwd_idx]) + c.fm[fwd_idx]) - 1);
-    }
-  }
-  __syncwarp();
-  for (u32 k = c.lane; k < n; k += 32) {
-    const u32 fwd_idx = c.fr[k];
-    const u32 f = c.fc[fwd_idx];
-    if (!cw_occurred_as(f, EV_PRIMARY)) continue;
-    const u32 rev_idx = cw_idx(f);
-    if (cw_occurred_as(c.rc[rev_idx], EV_LEF_BAR)) {
-      c.fm[fwd_idx] = (u32)((pos64(c.rev[rev_idx]) - c.rm[rev_idx]) - pos64(c.fwd[fwd_idx]) - 1);
-    }
-  }
-  __syncwarp();
 }
 
 // process_secondary_lef_lef_collisions (simulation_detect_collisions.cpp:404-518); lane 0
@@ -909,61 +749,845 @@ __device__ void process_secondary_serial(Cell& c, const KParams& P, u32 n, u64 n
   }
 }
 
+// One rev candidate of fix_secondary_lef_lef_collisions (simulation_detect_collisions.cpp:556-605).
+__device__ __forceinline__ void fix_rev_at(Cell& c, u64 start, u64 i) {
+  const u32 idx2 = c.rr[i];
+  const u32 idx1 = c.rr[i - 1];
+  const u64 pos1 = pos64(c.rev[idx1]) - c.rm[idx1];
+  const u64 r2 = pos64(c.rev[idx2]);
+  c.rm[idx2] = (r2 > pos1 + 1) ? (u32)(r2 - (pos1 + 1)) : 0u;
+  c.rc[idx2] = cw_make(idx1, EV_COLLISION | EV_SECONDARY);
+  const u64 p1 = pos64(c.rev[idx1]), p2 = r2;
+  c.rev[idx1] = (u32)min(pos64(c.fwd[idx1]), p2);
+  c.rev[idx2] = (u32)min(pos64(c.fwd[idx2]), p1);
+  u32 t = c.rc[idx1];
+  c.rc[idx1] = c.rc[idx2];
+  c.rc[idx2] = t;
+  t = c.rm[idx1];
+  c.rm[idx1] = c.rm[idx2];
+  c.rm[idx2] = t;
+  c.rr[i - 1] = idx2;
+  c.rr[i] = idx1;
+  c.rm[idx2] = (u32)min(pos64(c.rev[idx2]) - start, (u64)c.rm[idx2]);
+  c.rm[idx1] = (u32)min(pos64(c.rev[idx1]) - start, (u64)c.rm[idx1]);
+}
+
+// One fwd candidate (simulation_detect_collisions.cpp:608-646).
+__device__ __forceinline__ void fix_fwd_at(Cell& c, u64 end, u64 i) {
+  const u32 idx1 = c.fr[i];
+  const u32 idx2 = c.fr[i + 1];
+  const u64 f1 = pos64(c.fwd[idx1]);
+  const u64 pos2 = pos64(c.fwd[idx2]) + c.fm[idx2];
+  c.fm[idx1] = (pos2 > f1 + 1) ? (u32)(pos2 - (f1 + 1)) : 0u;
+  c.fc[idx1] = cw_make(idx2, EV_COLLISION | EV_SECONDARY);
+  const u64 p1 = f1, p2 = pos64(c.fwd[idx2]);
+  c.fwd[idx1] = (u32)max(pos64(c.rev[idx1]), p2);
+  c.fwd[idx2] = (u32)max(pos64(c.rev[idx2]), p1);
+  u32 t = c.fc[idx1];
+  c.fc[idx1] = c.fc[idx2];
+  c.fc[idx2] = t;
+  t = c.fm[idx1];
+  c.fm[idx1] = c.fm[idx2];
+  c.fm[idx2] = t;
+  c.fr[i] = idx2;
+  c.fr[i + 1] = idx1;
+  c.fm[idx2] = (u32)min(end - 1 - pos64(c.fwd[idx2]), (u64)c.fm[idx2]);
+  c.fm[idx1] = (u32)min(end - 1 - pos64(c.fwd[idx1]), (u64)c.fm[idx1]);
+}
+
 // fix_secondary_lef_lef_collisions (simulation_detect_collisions.cpp:520-647); lane 0
 __device__ void fix_secondary_serial(Cell& c, const KParams& P, u32 n, u64 n5, u64 n3) {
-  const u64 start = P.start, end = P.end;
   const u64 num_active_fwd = n - min(n3, n3 - 1);
   for (u64 i = max((u64)1, n5); i < n; ++i) {
-    const u32 idx2 = c.rr[i];
-    if (!cw_avoided_as(c.rc[idx2], EV_SECONDARY)) continue;
-    const u32 idx1 = c.rr[i - 1];
-    const u64 pos1 = pos64(c.rev[idx1]) - c.rm[idx1];
-    const u64 r2 = pos64(c.rev[idx2]);
-    c.rm[idx2] = (r2 > pos1 + 1) ? (u32)(r2 - (pos1 + 1)) : 0u;
-    c.rc[idx2] = cw_make(idx1, EV_COLLISION | EV_SECONDARY);
-    const u64 p1 = pos64(c.rev[idx1]), p2 = r2;
-    c.rev[idx1] = (u32)min(pos64(c.fwd[idx1]), p2);
-    c.rev[idx2] = (u32)min(pos64(c.fwd[idx2]), p1);
-    u32 t = c.rc[idx1];
-    c.rc[idx1] = c.rc[idx2];
-    c.rc[idx2] = t;
-    t = c.rm[idx1];
-    c.rm[idx1] = c.rm[idx2];
-    c.rm[idx2] = t;
-    c.rr[i - 1] = idx2;
-    c.rr[i] = idx1;
-    const u32 a = c.rr[i - 1], b = c.rr[i];
-    c.rm[a] = (u32)min(pos64(c.rev[a]) - start, (u64)c.rm[a]);
-    c.rm[b] = (u32)min(pos64(c.rev[b]) - start, (u64)c.rm[b]);
+    if (cw_avoided_as(c.rc[c.rr[i]], EV_SECONDARY)) fix_rev_at(c, P.start, i);
   }
   for (u64 i = 0; i + 1 < num_active_fwd; ++i) {
-    const u32 idx1 = c.fr[i];
-    if (!cw_avoided_as(c.fc[idx1], EV_SECONDARY)) continue;
-    const u32 idx2 = c.fr[i + 1];
-    const u64 f1 = pos64(c.fwd[idx1]);
-    const u64 pos2 = pos64(c.fwd[idx2]) + c.fm[idx2];
-    c.fm[idx1] = (pos2 > f1 + 1) ? (u32)(pos2 - (f1 + 1)) : 0u;
-    c.fc[idx1] = cw_make(idx2, EV_COLLISION | EV_SECONDARY);
-    const u64 p1 = f1, p2 = pos64(c.fwd[idx2]);
-    c.fwd[idx1] = (u32)max(pos64(c.rev[idx1]), p2);
-    c.fwd[idx2] = (u32)max(pos64(c.rev[idx2]), p1);
-    u32 t = c.fc[idx1];
-    c.fc[idx1] = c.fc[idx2];
-    c.fc[idx2] = t;
-    t = c.fm[idx1];
-    c.fm[idx1] = c.fm[idx2];
-    c.fm[idx2] = t;
-    c.fr[i] = idx2;
-    c.fr[i + 1] = idx1;
-    const u32 a = c.fr[i], b = c.fr[i + 1];
-    c.fm[a] = (u32)min(end - 1 - pos64(c.fwd[a]), (u64)c.fm[a]);
-    c.fm[b] = (u32)min(end - 1 - pos64(c.fwd[b]), (u64)c.fm[b]);
+    if (cw_avoided_as(c.fc[c.fr[i]], EV_SECONDARY)) fix_fwd_at(c, P.end, i);
   }
 }
 
-// extrude (simulation.cpp:489-512): warp-parallel
+
+// ---------------------------------------------------------------------------------------
+// Warp-parallel steps (all 32 lanes, uniform control flow)
+// ---------------------------------------------------------------------------------------
+
+// ExtrusionBarriers::init_states (extrusion_barriers.cpp:220-231)
+__device__ void barriers_init(Cell& c, u64* s) {
+  for (u32 base = 0; base < c.nb; base += 32) {
+    rng_ensure(c, s, 32);
+    const u32 i = base + ln();
+    const bool need = i < c.nb && (c.bar[i].flags & BF_OCC_DRAWS);
+    const unsigned m = __ballot_sync(FULL, need);
+    const u32 off = __popc(m & lanemask_lt());
+    bool occ = false;
+    if (need) occ = ring_at(c, c.sc->rpos + off) <= c.bar[i].t_occ;
+    const unsigned om = __ballot_sync(FULL, occ);
+    __syncwarp();
+    if (ln() == 0) {
+      c.bst[base >> 5] = om;
+      c.sc->rpos += __popc(m);
+    }
+    __syncwarp();
+  }
+}
+
+// ExtrusionBarriers::next_state (extrusion_barriers.cpp:145-161): one draw per barrier.
+__device__ void barriers_next(Cell& c, u64* s) {
+  for (u32 base = 0; base < c.nb; base += 32) {
+    rng_ensure(c, s, 32);
+    const u32 i = base + ln();
+    const bool valid = i < c.nb;
+    bool st = (c.bst[base >> 5] >> ln()) & 1u;
+    if (valid) {
+      const u64 u = ring_at(c, c.sc->rpos + ln());
+      const u32 f = c.bar[i].flags;
+      if (!st) {
+        st = !(f & BF_INA_NEVER) && u >= c.bar[i].t_ina;
+      } else {
+        st = !(!(f & BF_ACT_NEVER) && u >= c.bar[i].t_act);
+      }
+    }
+    const unsigned nm = __ballot_sync(FULL, valid && st);
+    __syncwarp();
+    if (ln() == 0) {
+      c.bst[base >> 5] = nm;
+      c.sc->rpos += min(32u, c.nb - base);
+    }
+    __syncwarp();
+  }
+}
+
+// select_lefs_to_bind + bind_lefs (simulation_impl.hpp:28-89): one uniform_int draw per
+// selected LEF in index order.  Selection: mode 0 = unbound LEFs (the epoch loop), 1 =
+// nonzero entries of mask, 2 = every LEF (an empty mask in the reference).
+__device__ __forceinline__ bool bind_selected(const Cell& c, u32 i, int mode, const u64* mask) {
+  return mode == 0 ? c.bep[i] == UNBOUND : (mode == 1 ? mask[i] != 0 : true);
+}
+
+__device__ void bind_lefs(Cell& c, u64* s, const KParams& P, u32 n, u32 epoch, int mode,
+                          const u64* mask) {
+  for (u32 i0 = 0; i0 < n; i0 += 32) {
+    rng_ensure(c, s, 32);
+    const u32 i = i0 + ln();
+    const bool need = i < n && bind_selected(c, i, mode, mask);
+    const unsigned m = __ballot_sync(FULL, need);
+    const u32 off = __popc(m & lanemask_lt());
+    u64 r = 0;
+    bool ok = true;
+    if (need) {
+      r = ring_at(c, c.sc->rpos + off) / P.pos_bucket;
+      ok = r <= P.pos_range;
+    }
+    const unsigned bad = __ballot_sync(FULL, need && !ok);
+    const u32 f = bad ? (u32)(__ffs(bad) - 1) : 32u;
+    if (need && ln() < f) {
+      const u32 pos = (u32)(P.start + r);
+      c.rev[i] = pos;
+      c.fwd[i] = pos;
+      c.bep[i] = epoch;
+    }
+    __syncwarp();
+    if (ln() == 0) {
+      c.sc->rpos += __popc(m & (f == 32 ? FULL : ((1u << f) - 1)));
+      if (f < 32) {  // finish this chunk serially from the rejecting LEF
+        for (u32 k = i0 + f; k < min(i0 + 32, n); ++k) {
+          if (!bind_selected(c, k, mode, mask)) continue;
+          const u64 pos = s_uniform_int(c, P.start, (u64)P.end - 1);
+          c.rev[k] = (u32)pos;
+          c.fwd[k] = (u32)pos;
+          c.bep[k] = epoch;
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// Ranking key of a unit: position, then binding epoch ascending (rev) or descending (fwd).
+__device__ __forceinline__ u64 rank_key(const Cell& c, u32 dir, u32 idx) {
+  const u32 p = dir ? c.fwd[idx] : c.rev[idx];
+  const u32 e = dir ? ~c.bep[idx] : c.bep[idx];
+  return ((u64)p << 32) | e;
+}
+
+// rank_lefs for one direction, warp-parallel.  The units bound this epoch (set M) are the
+// only ones whose positions jumped; the others (set S) keep the previous rank order.  If S
+// is still strictly increasing in (position, epoch key) and all keys are distinct, the
+// reference's result is the unique sorted order, built here as a merge of S with sorted M.
+// Returns false (nothing written) when that does not hold: the caller then runs the exact
+// split_sort / pdq_sort emulation.
+__device__ bool rank_dir_fast(Cell& c, u32 dir, u32 n, u32 epoch) {
+  u32* R = dir ? c.fr : c.rr;
+  u32* Sidx = c.sr;
+  u32* Midx = c.tmp;
+  u32* Msort = c.sf;
+  u32 ns = 0, nm = 0;
+  for (u32 base = 0; base < n; base += 32) {
+    const u32 i = base + ln();
+    const bool valid = i < n;
+    const u32 idx = valid ? R[i] : 0;
+    const bool isM = valid && c.bep[idx] == epoch;
+    const bool isS = valid && !isM;
+    const unsigned ms = __ballot_sync(FULL, isS), mm = __ballot_sync(FULL, isM);
+    if (isS) Sidx[ns + __popc(ms & lanemask_lt())] = idx;
+    if (isM) Midx[nm + __popc(mm & lanemask_lt())] = idx;
+    ns += __popc(ms);
+    nm += __popc(mm);
+  }
+  __syncwarp();
+  if (nm > 1024) return false;
+  bool bad = false;
+  for (u32 k = ln() + 1; k < ns; k += 32) {
+    if (!(rank_key(c, dir, Sidx[k - 1]) < rank_key(c, dir, Sidx[k]))) bad = true;
+  }
+  if (__any_sync(FULL, bad)) return false;
+  // sort M by counting ranks; distinct keys required
+  for (u32 a = ln(); a < nm; a += 32) {
+    const u64 ka = rank_key(c, dir, Midx[a]);
+    u32 r = 0;
+    for (u32 b = 0; b < nm; ++b) {
+      const u64 kb = rank_key(c, dir, Midx[b]);
+      r += kb < ka;
+      bad |= (kb == ka) && (b != a);
+    }
+    if (!bad) Msort[r] = Midx[a];
+  }
+  if (__any_sync(FULL, bad)) return false;
+  __syncwarp();
+  // no M key may equal an S key
+  for (u32 m = ln(); m < nm; m += 32) {
+    const u64 km = rank_key(c, dir, Msort[m]);
+    u32 lo = 0, hi = ns;
+    while (lo < hi) {
+      const u32 mid = (lo + hi) >> 1;
+      if (rank_key(c, dir, Sidx[mid]) < km) lo = mid + 1; else hi = mid;
+    }
+    if (lo < ns && rank_key(c, dir, Sidx[lo]) == km) bad = true;
+  }
+  if (__any_sync(FULL, bad)) return false;
+  // merge
+  for (u32 sidx = ln(); sidx < ns; sidx += 32) {
+    const u32 idx = Sidx[sidx];
+    const u64 ks = rank_key(c, dir, idx);
+    u32 lo = 0, hi = nm;
+    while (lo < hi) {
+      const u32 mid = (lo + hi) >> 1;
+      if (rank_key(c, dir, Msort[mid]) < ks) lo = mid + 1; else hi = mid;
+    }
+    R[sidx + lo] = idx;
+  }
+  for (u32 m = ln(); m < nm; m += 32) {
+    const u32 idx = Msort[m];
+    const u64 km = rank_key(c, dir, idx);
+    u32 lo = 0, hi = ns;
+    while (lo < hi) {
+      const u32 mid = (lo + hi) >> 1;
+      if (rank_key(c, dir, Sidx[mid]) < km) lo = mid + 1; else hi = mid;
+    }
+    R[m + lo] = idx;
+  }
+  __syncwarp();
+  return true;
+}
+
+__device__ void rank_lefs(Cell& c, const KParams& P, u32 n, u32 epoch, bool partially_sorted) {
+  for (u32 dir = 0; dir < 2; ++dir) {
+    const bool ok = !(P.debug_flags & DBG_SERIAL_RANK) && rank_dir_fast(c, dir, n, epoch);
+    if (!ok) {
+      if (ln() == 0) {
+        rank_dir_serial(c, dir, n, partially_sorted);
+        c.sc->sort_fallbacks++;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// positions in rank order: sr[k] = rev[rr[k]], sf[k] = fwd[fr[k]]
+__device__ void gather_ranked(Cell& c, u32 n) {
+  for (u32 k = ln(); k < n; k += 32) {
+    c.sr[k] = c.rev[c.rr[k]];
+    c.sf[k] = c.fwd[c.fr[k]];
+  }
+  __syncwarp();
+}
+
+// generate_moves_helper (simulation.cpp:264-290): speculation on the ziggurat fast path; the
+// first item that needs more draws is finished serially by lane 0.
+__device__ __forceinline__ bool normal_fast(u64 u, double& z);
+__device__ double s_unit_normal(Cell& c);
+
+__device__ void gen_moves_dir(Cell& c, u64* s, u32* mv, u32 n, double mean, double sd, u64 move_int) {
+  if (sd == 0.0) {
+    for (u32 i = ln(); i < n; i += 32) mv[i] = c.bep[i] == UNBOUND ? 0u : (u32)move_int;
+    __syncwarp();
+    return;
+  }
+  u32 i0 = 0;
+  while (i0 < n) {
+    rng_ensure(c, s, 64);
+    const u32 i = i0 + ln();
+    const bool need = i < n && c.bep[i] != UNBOUND;
+    const unsigned m = __ballot_sync(FULL, need);
+    const u32 off = __popc(m & lanemask_lt());
+    double z = 0;
+    bool ok = true;
+    if (need) ok = normal_fast(ring_at(c, c.sc->rpos + off), z);
+    const unsigned bad = __ballot_sync(FULL, need && !ok);
+    const u32 f = bad ? (u32)(__ffs(bad) - 1) : 32u;
+    if (i < n && ln() < f) {
+      if (need) {
+        const double v = round(fmax(0.0, z * sd + mean));
+        if (v > 4294967295.0) set_status(c, DEV_ERR_MOVE_RANGE);
+        mv[i] = (u32)(u64)v;
+      } else {
+        mv[i] = 0;
+      }
+    }
+    __syncwarp();
+    if (ln() == 0) {
+      c.sc->rpos += __popc(m & (f == 32 ? FULL : ((1u << f) - 1)));
+      if (f < 32) {
+        const double zz = s_unit_normal(c);
+        const double v = round(fmax(0.0, zz * sd + mean));
+        if (v > 4294967295.0) set_status(c, DEV_ERR_MOVE_RANGE);
+        mv[i0 + f] = (u32)(u64)v;
+      }
+    }
+    __syncwarp();
+    i0 += (f == 32) ? 32 : f + 1;
+  }
+}
+
+// adjust_moves_of_consecutive_extr_units, rev units: pairs (k, k+1) from the top rank down.
+// With t_k = pos_k - move_k the reference computes T_k = min(t_k, T_{k+1} - 1) when the pair
+// links (both bound, t_k > start, T_{k+1} > start), else T_k = t_k.  In U_k = T_k - k this is
+// a segmented suffix minimum.  The scan takes the static part of the link condition; the
+// dynamic part (T_{k+1} > start) is checked afterwards and a failure anywhere rejects the
+// result (serial fallback).  New moves go to tmp first and are copied only on success.
+__device__ bool adjust_rev_fast(Cell& c, const KParams& P, u32 n) {
+  const i64 start = P.start;
+  u32* out = c.tmp;
+  i64 carry_u = 0;       // U of element kb + 32
+  bool carry_b = false;  // bound flag of element kb + 32
+  bool bad = false;
+  for (i64 kb = ((i64)n - 1) / 32 * 32; kb >= 0; kb -= 32) {
+    const i64 k = kb + ln();
+    const bool valid = k < (i64)n;
+    const u32 idx = valid ? c.rr[k] : 0;
+    const bool b = valid && c.bep[idx] != UNBOUND;
+    const i64 p = valid ? (i64)c.sr[k] : 0;
+    const i64 t = valid ? p - (i64)c.rm[idx] : 0;
+    bool b_next = __shfl_down_sync(FULL, b, 1);
+    if (ln() == 31) b_next = carry_b;
+    const bool link_next = valid && k + 1 < (i64)n && b && b_next && t > start;
+    i64 v = t - k;
+    bool stop = !link_next;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const i64 vr = __shfl_down_sync(FULL, v, d);
+      const bool sr_ = __shfl_down_sync(FULL, stop, d);
+      if ((int)ln() + d < 32 && !stop) {
+        v = min(v, vr);
+        stop = sr_;
+      }
+    }
+    if (valid && !stop) v = min(v, carry_u);  // linked through lane 31 to element kb + 32
+    const i64 T = v + k;
+    i64 T_next = __shfl_down_sync(FULL, T, 1);
+    if (ln() == 31) T_next = carry_u + kb + 32;
+    if (link_next && T_next <= start) bad = true;  // the reference would skip this pair
+    if (valid) out[k] = (u32)(p - T);
+    carry_u = __shfl_sync(FULL, v, 0);
+    carry_b = __shfl_sync(FULL, b, 0);
+  }
+  if (__any_sync(FULL, bad)) return false;
+  __syncwarp();
+  for (u32 k = ln(); k < n; k += 32) c.rm[c.rr[k]] = out[k];
+  __syncwarp();
+  return true;
+}
+
+// fwd units: pairs (k-1, k) from the bottom rank up; T_k = max(t_k, T_{k-1} + 1) when linked
+// (both bound, t_k <= end - 1, T_{k-1} <= end - 1); V_k = T_k - k is a segmented prefix max.
+__device__ bool adjust_fwd_fast(Cell& c, const KParams& P, u32 n) {
+  const i64 endm1 = (i64)P.end - 1;
+  u32* out = c.tmp;
+  i64 carry_v = 0;       // V of element kb - 1
+  bool carry_b = false;  // bound flag of element kb - 1
+  bool bad = false;
+  for (u32 kb = 0; kb < n; kb += 32) {
+    const i64 k = (i64)kb + ln();
+    const bool valid = k < (i64)n;
+    const u32 idx = valid ? c.fr[k] : 0;
+    const bool b = valid && c.bep[idx] != UNBOUND;
+    const i64 p = valid ? (i64)c.sf[k] : 0;
+    const i64 t = valid ? p + (i64)c.fm[idx] : 0;
+    bool b_prev = __shfl_up_sync(FULL, b, 1);
+    if (ln() == 0) b_prev = carry_b;
+    const bool link_prev = valid && k > 0 && b && b_prev && t <= endm1;
+    i64 v = t - k;
+    bool stop = !link_prev;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const i64 vl = __shfl_up_sync(FULL, v, d);
+      const bool sl = __shfl_up_sync(FULL, stop, d);
+      if ((int)ln() >= d && !stop) {
+        v = max(v, vl);
+        stop = sl;
+      }
+    }
+    if (valid && !stop) v = max(v, carry_v);  // linked through lane 0 to element kb - 1
+    const i64 T = v + k;
+    i64 T_prev = __shfl_up_sync(FULL, T, 1);
+    if (ln() == 0) T_prev = carry_v + (i64)kb - 1;
+    if (link_prev && T_prev > endm1) bad = true;
+    if (valid) out[k] = (u32)(T - p);
+    carry_v = __shfl_sync(FULL, v, 31);
+    carry_b = __shfl_sync(FULL, b, 31);
+  }
+  if (__any_sync(FULL, bad)) return false;
+  __syncwarp();
+  for (u32 k = ln(); k < n; k += 32) c.fm[c.fr[k]] = out[k];
+  __syncwarp();
+  return true;
+}
+
+__device__ void adjust_moves(Cell& c, const KParams& P, u32 n) {
+  const bool serial = P.debug_flags & DBG_SERIAL_ADJUST;
+  if (serial || !adjust_rev_fast(c, P, n)) {
+    if (ln() == 0) adjust_dir_serial(c, P, 0, n);
+    __syncwarp();
+  }
+  if (serial || !adjust_fwd_fast(c, P, n)) {
+    if (ln() == 0) adjust_dir_serial(c, P, 1, n);
+    __syncwarp();
+  }
+}
+
+// clamp_moves (simulation.cpp:325-340)
+__device__ void clamp_moves(Cell& c, const KParams& P, u32 n) {
+  for (u32 i = ln(); i < n; i += 32) {
+    if (c.bep[i] == UNBOUND) continue;
+    const u64 rmv = min((u64)c.rm[i], pos64(c.rev[i]) - P.start);
+    const u64 fmv = min((u64)c.fm[i], (u64)P.end - pos64(c.fwd[i]) - 1);
+    c.rm[i] = (u32)rmv;
+    c.fm[i] = (u32)fmv;
+  }
+  __syncwarp();
+}
+
+// ranked positions sorted (non-decreasing)?  Needed by the closed forms below; the epoch loop
+// always satisfies it, caller-provided ranks may not.
+__device__ bool ranked_sorted(const Cell& c, u32 n) {
+  bool bad = false;
+  for (u32 k = ln() + 1; k < n; k += 32) {
+    if (c.sr[k - 1] > c.sr[k] || c.sf[k - 1] > c.sf[k]) bad = true;
+  }
+  return !__any_sync(FULL, bad);
+}
+
+// Bernoulli trial of one lane with the draw at its offset (or none).
+__device__ __forceinline__ bool trial_needs_draw(const Trial& t) { return !t.always && t.draws; }
+__device__ __forceinline__ bool trial_outcome(const Trial& t, u64 u) {
+  if (t.always) return true;
+  if (!t.draws) return false;
+  return u <= t.thr;
+}
+
+// detect_lef_bar_collisions (simulation_detect_collisions.cpp:128-252), warp-parallel.  For
+// an occupied barrier the reference's sweep tests the first rev unit (in rank order, from
+// index max(n5 - 1, 0)) strictly downstream of it and the last fwd unit strictly upstream of
+// it (up to index n - max(n3 - 1, 0) - 1): binary searches over the ranked positions.
+// Trials draw in barrier order (ascending for rev units, descending for fwd units); a unit
+// hit by several barriers keeps the last successful one in that order.
+__device__ void detect_lef_bar_fast(Cell& c, u64* s, const KParams& P, u32 n, u64 n5, u64 n3) {
+  const u32 j0 = (u32)min(n5, n5 - 1);
+  for (u32 base = 0; base < c.nb; base += 32) {
+    rng_ensure(c, s, 32);
+    const u32 i = base + ln();
+    bool cand = false, drawn = false;
+    u32 unit = 0;
+    if (i < c.nb && bar_active(c, i)) {
+      const u32 bpos = c.bar[i].pos;
+      u32 lo = j0, hi = n;  // first k in [j0, n) with sr[k] > bpos
+      while (lo < hi) {
+        const u32 mid = (lo + hi) >> 1;
+        if (c.sr[mid] > bpos) hi = mid; else lo = mid + 1;
+      }
+      if (lo < n) {
+        unit = c.rr[lo];
+        if (c.bep[unit] != UNBOUND) {
+          const u64 delta = (u64)c.sr[lo] - bpos;
+          const Trial& tr = P.lef_bar[(c.bar[i].flags & BF_DIR_MASK) == MGPU_DIR_REV ? 0 : 1];
+          if (delta > 0 && delta <= c.rm[unit]) {
+            cand = true;
+            drawn = trial_needs_draw(tr);
+          }
+        }
+      }
+    }
+    const unsigned dm = __ballot_sync(FULL, drawn);
+    bool hit = false;
+    if (cand) {
+      const Trial& tr = P.lef_bar[(c.bar[i].flags & BF_DIR_MASK) == MGPU_DIR_REV ? 0 : 1];
+      const u64 u = drawn ? ring_at(c, c.sc->rpos + __popc(dm & lanemask_lt())) : 0;
+      hit = trial_outcome(tr, u);
+    }
+    // the highest barrier index wins among this chunk's hits on the same unit
+    const unsigned hm = __ballot_sync(FULL, hit);
+    const unsigned same = __match_any_sync(FULL, hit ? unit : 0xFFFFFFFFu);
+    if (hit && (31 - __clz(same & hm)) == (int)ln()) c.rc[unit] = cw_make(i, EV_COLLISION | EV_LEF_BAR);
+    __syncwarp();
+    if (ln() == 0) c.sc->rpos += __popc(dm);
+    __syncwarp();
+  }
+  const u32 jtop = (u32)(n - min(n3, n3 - 1)) - 1;  // last fwd rank index searched
+  for (i64 top = (i64)c.nb - 1; top >= 0; top -= 32) {
+    rng_ensure(c, s, 32);
+    const i64 ii = top - (i64)ln();
+    bool cand = false, drawn = false;
+    u32 unit = 0;
+    if (ii >= 0 && bar_active(c, (u32)ii)) {
+      const u32 bpos = c.bar[ii].pos;
+      u32 lo = 0, hi = jtop + 1;  // first k in [0, jtop] with sf[k] >= bpos
+      while (lo < hi) {
+        const u32 mid = (lo + hi) >> 1;
+        if (c.sf[mid] >= bpos) hi = mid; else lo = mid + 1;
+      }
+      if (lo > 0) {
+        const u32 k = lo - 1;
+        unit = c.fr[k];
+        if (c.bep[unit] != UNBOUND) {
+          const u64 delta = (u64)bpos - c.sf[k];
+          const Trial& tr = P.lef_bar[(c.bar[ii].flags & BF_DIR_MASK) == MGPU_DIR_FWD ? 0 : 1];
+          if (delta > 0 && delta <= c.fm[unit]) {
+            cand = true;
+            drawn = trial_needs_draw(tr);
+          }
+        }
+      }
+    }
+    const unsigned dm = __ballot_sync(FULL, drawn);
+    bool hit = false;
+    if (cand) {
+      const Trial& tr = P.lef_bar[(c.bar[ii].flags & BF_DIR_MASK) == MGPU_DIR_FWD ? 0 : 1];
+      const u64 u = drawn ? ring_at(c, c.sc->rpos + __popc(dm & lanemask_lt())) : 0;
+      hit = trial_outcome(tr, u);
+    }
+    // loop order is descending barrier index: the last hit on a unit is the highest lane
+    const unsigned hm = __ballot_sync(FULL, hit);
+    const unsigned same = __match_any_sync(FULL, hit ? unit : 0xFFFFFFFFu);
+    if (hit && (31 - __clz(same & hm)) == (int)ln()) c.fc[unit] = cw_make((u32)ii, EV_COLLISION | EV_LEF_BAR);
+    __syncwarp();
+    if (ln() == 0) c.sc->rpos += __popc(dm);
+    __syncwarp();
+  }
+}
+
+// detect_primary_lef_lef_collisions (simulation_detect_collisions.cpp:255-401), warp-parallel.
+// With cnt(j) = number of fwd units (rank < i2) strictly before rev unit j, the sweep tests
+// exactly the rev units j >= n5 with cnt(j) > cnt(j - 1) (cnt(n5 - 1) := 0) and cnt(j) < i2,
+// each against the fwd unit of rank cnt(j) - 1.  Tested pairs are disjoint, so their
+// collision words are updated independently; trials draw in ascending j.
+__device__ void detect_primary_fast(Cell& c, u64* s, const KParams& P, u32 n, u64 n5, u64 n3) {
+  if (n5 == n || n3 == n) return;
+  const u32 i2 = (u32)(n - min(n3, n3 - 1));
+  u32 carry = 0;  // cnt of the element before the chunk
+  for (u32 base = (u32)n5; base < n; base += 32) {
+    rng_ensure(c, s, 32);
+    const u32 j = base + ln();
+    const bool valid = j < n;
+    u32 cnt = 0;
+    if (valid) {
+      const u32 rp = c.sr[j];
+      u32 lo = 0, hi = i2;  // first i in [0, i2) with sf[i] >= rp
+      while (lo < hi) {
+        const u32 mid = (lo + hi) >> 1;
+        if (c.sf[mid] >= rp) hi = mid; else lo = mid + 1;
+      }
+      cnt = lo;
+    }
+    u32 prev = __shfl_up_sync(FULL, cnt, 1);
+    if (ln() == 0) prev = carry;
+    const bool tested = valid && cnt > prev && cnt < i2;
+    u32 rev_idx = 0, fwd_idx = 0;
+    u64 rmv = 0, fmv = 0, rp = 0, fp = 0;
+    bool cand = false;
+    if (tested) {
+      rev_idx = c.rr[j];
+      fwd_idx = c.fr[cnt - 1];
+      rp = pos64(c.sr[j]);
+      fp = pos64(c.sf[cnt - 1]);
+      rmv = c.rm[rev_idx];
+      fmv = c.fm[fwd_idx];
+      const u64 delta = rp - fp;
+      cand = delta > 0 && delta < rmv + fmv;
+    }
+    const bool drawn = cand && trial_needs_draw(P.lef_lef);
+    const unsigned dm = __ballot_sync(FULL, drawn);
+    bool hit = false;
+    if (cand) hit = trial_outcome(P.lef_lef, drawn ? ring_at(c, c.sc->rpos + __popc(dm & lanemask_lt())) : 0);
+    if (hit) primary_pair_update(c, rev_idx, fwd_idx, rp, fp, rmv, fmv);
+    carry = __shfl_sync(FULL, cnt, 31);
+    __syncwarp();
+    if (ln() == 0) c.sc->rpos += __popc(dm);
+    __syncwarp();
+  }
+}
+
+// correct_moves_for_lef_bar_collisions (simulation_correct_moves.cpp:20-51)
+__device__ void correct_lef_bar(Cell& c, u32 n) {
+  for (u32 i = ln(); i < n; i += 32) {
+    const u32 r = c.rc[i], f = c.fc[i];
+    if (cw_occurred_as(r, EV_LEF_BAR)) c.rm[i] = (u32)(pos64(c.rev[i]) - c.bar[cw_idx(r)].pos - 1);
+    if (cw_occurred_as(f, EV_LEF_BAR)) c.fm[i] = (u32)(c.bar[cw_idx(f)].pos - pos64(c.fwd[i]) - 1);
+  }
+  __syncwarp();
+}
+
+// correct_moves_for_primary_lef_lef_collisions (simulation_correct_moves.cpp:54-122): the
+// pairs it visits are disjoint, so both passes are warp-parallel.
+__device__ void correct_primary(Cell& c, u32 n) {
+  for (u32 k = ln(); k < n; k += 32) {
+    const u32 rev_idx = c.rr[k];
+    const u32 r = c.rc[rev_idx];
+    if (!cw_occurred_as(r, EV_PRIMARY)) continue;
+    const u32 fwd_idx = cw_idx(r);
+    const u32 f = c.fc[fwd_idx];
+    if (cw_occurred_as(f, EV_PRIMARY)) {
+      const u64 rp = pos64(c.rev[rev_idx]), fp = pos64(c.fwd[fwd_idx]);
+      u64 p1, p2;
+      lef_lef_collision_pos(rp, fp, c.rm[rev_idx], c.fm[fwd_idx], p1, p2);
+      c.rm[rev_idx] = (u32)(rp - p1);
+      c.fm[fwd_idx] = (u32)(p2 - fp);
+    } else if (cw_occurred_as(f, EV_LEF_BAR)) {
+      c.rm[rev_idx] = (u32)(pos64(c.rev[rev_idx]) - (pos64(c.fwd[fwd_idx]) + c.fm[fwd_idx]) - 1);
+    }
+  }
+  __syncwarp();
+  for (u32 k = ln(); k < n; k += 32) {
+    const u32 fwd_idx = c.fr[k];
+    const u32 f = c.fc[fwd_idx];
+    if (!cw_occurred_as(f, EV_PRIMARY)) continue;
+    const u32 rev_idx = cw_idx(f);
+    if (cw_occurred_as(c.rc[rev_idx], EV_LEF_BAR)) {
+      c.fm[fwd_idx] = (u32)((pos64(c.rev[rev_idx]) - c.rm[rev_idx]) - pos64(c.fwd[fwd_idx]) - 1);
+    }
+  }
+  __syncwarp();
+}
+
+// process_secondary_lef_lef_collisions (simulation_detect_collisions.cpp:404-518), warp-parallel.
+// A stalled unit followed (rev: in rank order; fwd: in reverse rank order) by free units
+// starts a chain: each free unit whose target passes its stalled predecessor's target draws a
+// bypass trial; success stalls it one bp behind (extending the chain), failure marks it
+// avoided and ends the chain.  Chains lie between units that were stalled on entry, so they
+// are disjoint and one lane walks one chain.  Draw offsets assume every trial succeeds; the
+// first chain whose trial fails shifts the later ones, so the warp commits up to it and
+// resumes after it.  dir 0: rev units (chains ascend), dir 1: fwd units (chains descend).
+enum ChainMode { CHAIN_COUNT = 0, CHAIN_RING = 1, CHAIN_SERIAL = 2 };
+
+template <int MODE>
+__device__ __forceinline__ u32 chain_walk(Cell& c, const KParams& P, u32 dir, u32 n, i64 k,
+                                          u64 off, u32* used_out) {
+  const Trial& tr = P.lef_lef;
+  const u32* R = dir ? c.fr : c.rr;
+  u32* M = dir ? c.fm : c.rm;
+  u32* C = dir ? c.fc : c.rc;
+  const u32* S = dir ? c.sf : c.sr;
+  const i64 step = dir ? -1 : 1;
+  const i64 stop = dir ? -1 : (i64)n;
+  u32 idx_prev = R[k - step];
+  u64 tprev = dir ? pos64(S[k - step]) + M[idx_prev] : pos64(S[k - step]) - M[idx_prev];
+  u32 used = 0, trials = 0;
+  for (; k != stop; k += step) {
+    const u32 idx = R[k];
+    if (cw_occurred(C[idx])) break;  // stalled on entry: the next chain starts after it
+    const u64 p = pos64(S[k]);
+    const u64 m = M[idx];
+    if (!(dir ? (p + m >= tprev) : (p - m <= tprev))) break;
+    bool ok;
+    if (tr.always) {
+      ok = true;
+    } else if (!tr.draws) {
+      ok = false;
+    } else {
+      u64 u = 0;
+      if (MODE == CHAIN_RING) u = ring_at(c, c.sc->rpos + off + used);
+      if (MODE == CHAIN_SERIAL) u = rng_serial(c);
+      ok = MODE == CHAIN_COUNT || u <= tr.thr;
+      ++used;
+    }
+    ++trials;
+    if (!ok) {
+      if (MODE != CHAIN_COUNT) C[idx] = cw_make(idx_prev, EV_SECONDARY);
+      break;
+    }
+    const u64 mv = dir ? (tprev - p) : (p - tprev);
+    const u64 m2 = min(mv, mv - 1);
+    if (MODE != CHAIN_COUNT) {
+      C[idx] = cw_make(idx_prev, EV_COLLISION | EV_SECONDARY);
+      M[idx] = (u32)m2;
+    }
+    tprev = dir ? p + m2 : p - m2;
+    idx_prev = idx;
+  }
+  *used_out = used;
+  return trials;
+}
+
+__device__ void secondary_dir_fast(Cell& c, u64* s, const KParams& P, u32 dir, u32 n, u64 n5, u64 n3) {
+  const u32* R = dir ? c.fr : c.rr;
+  const u32* C = dir ? c.fc : c.rc;
+  // chain starts (index of the first free unit): rev: k in [max(1, n5), n) with R[k-1]
+  // stalled and R[k] free, ascending; fwd: k = i - 1 for i in [1, itop] with R[i] stalled
+  // and R[k] free, in descending i
+  u32* starts = c.tmp;
+  u32 nst = 0;
+  if (dir == 0) {
+    for (u32 base = (u32)max((u64)1, n5); base < n; base += 32) {
+      const u32 k = base + ln();
+      const bool st = k < n && cw_occurred(C[R[k - 1]]) && !cw_occurred(C[R[k]]);
+      const unsigned m = __ballot_sync(FULL, st);
+      if (st) starts[nst + __popc(m & lanemask_lt())] = k;
+      nst += __popc(m);
+    }
+  } else {
+    const i64 itop = (i64)(n - min(n3, n3 - 1)) - 1;
+    for (i64 top = itop; top >= 1; top -= 32) {
+      const i64 i = top - (i64)ln();
+      const bool st = i >= 1 && cw_occurred(C[R[i]]) && !cw_occurred(C[R[i - 1]]);
+      const unsigned m = __ballot_sync(FULL, st);
+      if (st) starts[nst + __popc(m & lanemask_lt())] = (u32)(i - 1);
+      nst += __popc(m);
+    }
+  }
+  __syncwarp();
+  const bool draws = trial_needs_draw(P.lef_lef);
+  u32 q = 0;
+  while (q < nst) {
+    rng_ensure(c, s, RNG_BLOCK);
+    const u32 ci = q + ln();
+    u32 L = 0, unused;
+    if (ci < nst) L = chain_walk<CHAIN_COUNT>(c, P, dir, n, starts[ci], 0, &unused);
+    const u32 Ld = draws ? L : 0;
+    u32 tot;
+    const u32 off = warp_excl_scan(Ld, &tot);
+    // lanes whose speculative window would run past the draws known to be in the ring
+    const unsigned over = __ballot_sync(FULL, ci < nst && off + Ld > RNG_BLOCK);
+    const u32 fb = over ? (u32)(__ffs(over) - 1) : 32u;
+    if (fb == 0) {  // a single chain longer than the ring window: walk it serially
+      if (ln() == 0) {
+        u32 used;
+        chain_walk<CHAIN_SERIAL>(c, P, dir, n, starts[q], 0, &used);
+      }
+      __syncwarp();
+      q += 1;
+      continue;
+    }
+    // evaluate each chain's trials at its speculative offset
+    u32 used = 0;
+    bool fails = false;
+    if (ci < nst && ln() < fb && Ld > 0) {
+      u32 k = 0;
+      while (k < Ld && ring_at(c, c.sc->rpos + off + k) <= P.lef_lef.thr) ++k;
+      fails = k < Ld;
+      used = fails ? k + 1 : Ld;
+    } else {
+      used = Ld;
+    }
+    const unsigned fm_ = __ballot_sync(FULL, fails);
+    const u32 f = fm_ ? (u32)(__ffs(fm_) - 1) : 32u;  // first chain whose trial fails
+    const u32 last = min(f == 32 ? 31u : f, fb - 1);   // commit chains q .. q + last
+    if (ci < nst && ln() <= last) {
+      u32 u2;
+      chain_walk<CHAIN_RING>(c, P, dir, n, starts[ci], off, &u2);
+    }
+    const u32 consumed = __shfl_sync(FULL, off + used, last);
+    __syncwarp();
+    if (ln() == 0) c.sc->rpos += consumed;
+    __syncwarp();
+    q += last + 1;
+  }
+}
+
+// fix_secondary_lef_lef_collisions, warp-parallel: candidates (units marked avoided) are never
+// adjacent in rank order (the unit before a rev candidate, after a fwd candidate, is stalled),
+// so each is an independent swap of two neighbours.
+__device__ bool fix_secondary_fast(Cell& c, const KParams& P, u32 n, u64 n5, u64 n3) {
+  const u64 k0 = max((u64)1, n5);
+  bool adj = false;
+  for (u64 i = k0 + ln(); i < n; i += 32) {
+    if (cw_avoided_as(c.rc[c.rr[i]], EV_SECONDARY) && i + 1 < n &&
+        cw_avoided_as(c.rc[c.rr[i + 1]], EV_SECONDARY))
+      adj = true;
+  }
+  const u64 naf = n - min(n3, n3 - 1);
+  for (u64 i = ln(); i + 1 < naf; i += 32) {
+    if (cw_avoided_as(c.fc[c.fr[i]], EV_SECONDARY) && i + 2 < naf &&
+        cw_avoided_as(c.fc[c.fr[i + 1]], EV_SECONDARY))
+      adj = true;
+  }
+  if (__any_sync(FULL, adj)) return false;
+  __syncwarp();
+  for (u64 i = k0 + ln(); i < n; i += 32) {
+    if (cw_avoided_as(c.rc[c.rr[i]], EV_SECONDARY)) fix_rev_at(c, P.start, i);
+  }
+  __syncwarp();
+  for (u64 i = ln(); i + 1 < naf; i += 32) {
+    if (cw_avoided_as(c.fc[c.fr[i]], EV_SECONDARY)) fix_fwd_at(c, P.end, i);
+  }
+  __syncwarp();
+  return true;
+}
+
+// process_collisions (simulation.cpp:925-955) in the reference's order.
+__device__ void process_collisions(Cell& c, u64* s, const KParams& P, u32 n, bool fix) {
+  Scalars* sc = c.sc;
+  const bool serial = (P.debug_flags & DBG_SERIAL_COLLISIONS) || !ranked_sorted(c, n);
+  __syncwarp();
+  if (ln() == 0) {
+    u64 n5, n3;
+    detect_boundaries_serial(c, P, n, n5, n3);
+    sc->n5 = n5;
+    sc->n3 = n3;
+  }
+  __syncwarp();
+  const u64 n5 = sc->n5, n3 = sc->n3;
+  if (serial) {
+    rng_ensure(c, s, RNG_BLOCK);
+    if (ln() == 0) {
+      detect_lef_bar_serial(c, P, n, n5, n3);
+      detect_primary_serial(c, P, n, n5, n3);
+    }
+    __syncwarp();
+  } else {
+    detect_lef_bar_fast(c, s, P, n, n5, n3);
+    detect_primary_fast(c, s, P, n, n5, n3);
+  }
+  correct_lef_bar(c, n);
+  correct_primary(c, n);
+  if (serial) {
+    rng_ensure(c, s, RNG_BLOCK);
+    if (ln() == 0) process_secondary_serial(c, P, n, n5, n3);
+    __syncwarp();
+  } else {
+    // chains read ranked positions; secondary moves only change moves and words
+    secondary_dir_fast(c, s, P, 0, n, n5, n3);
+    secondary_dir_fast(c, s, P, 1, n, n5, n3);
+  }
+  if (fix) {
+    if (serial || !fix_secondary_fast(c, P, n, n5, n3)) {
+      if (ln() == 0) fix_secondary_serial(c, P, n, n5, n3);
+      __syncwarp();
+    }
+  }
+}
+
+// extrude (simulation.cpp:489-512)
 __device__ void extrude(Cell& c, u32 n) {
-  for (u32 i = c.lane; i < n; i += 32) {
+  for (u32 i = ln(); i < n; i += 32) {
     if (c.bep[i] == UNBOUND) continue;
     c.rev[i] -= c.rm[i];
     c.fwd[i] += c.fm[i];
@@ -971,12 +1595,12 @@ __device__ void extrude(Cell& c, u32 n) {
   __syncwarp();
 }
 
-// release_lefs (simulation.cpp:544-592): warp-parallel, one draw per bound LEF with p > 0.
-__device__ u32 release_lefs(Cell& c, const KParams& P, u32 n, bool completed) {
+// release_lefs (simulation.cpp:544-592): one draw per bound LEF with p > 0.
+__device__ u32 release_lefs(Cell& c, u64* s, const KParams& P, u32 n, bool completed) {
   u32 released = 0;
   for (u32 base = 0; base < n; base += 32) {
-    rng_ensure(c, 32);
-    const u32 i = base + c.lane;
+    rng_ensure(c, s, 32);
+    const u32 i = base + ln();
     const bool bound = i < n && c.bep[i] != UNBOUND;
     Trial tr{0, 0, 0};
     if (bound) {
@@ -987,7 +1611,7 @@ __device__ u32 release_lefs(Cell& c, const KParams& P, u32 n, bool completed) {
       tr = P.release[completed ? 1 : 0][nh];
     }
     const bool need = bound && tr.draws;
-    const unsigned m = __ballot_sync(0xFFFFFFFFu, need);
+    const unsigned m = __ballot_sync(FULL, need);
     const u32 off = __popc(m & lanemask_lt());
     const bool rel = need && ring_at(c, c.sc->rpos + off) <= tr.thr;
     if (rel) {
@@ -995,30 +1619,44 @@ __device__ u32 release_lefs(Cell& c, const KParams& P, u32 n, bool completed) {
       c.fwd[i] = UNBOUND;
       c.bep[i] = UNBOUND;
     }
-    released += __popc(__ballot_sync(0xFFFFFFFFu, rel));
+    released += __popc(__ballot_sync(FULL, rel));
     __syncwarp();
-    if (c.lane == 0) c.sc->rpos += __popc(m);
+    if (ln() == 0) c.sc->rpos += __popc(m);
     __syncwarp();
   }
   return released;
 }
 
-// compute_loop_size_stats + evaluate_burnin (simulation.cpp:957-1025); lane 0.
-__device__ bool burnin_stats_serial(Cell& c, const KParams& P, u32 n) {
+// compute_loop_size_stats + evaluate_burnin (simulation.cpp:957-1025).  Loop sizes are
+// integers below 2^32, so the reference's double sum is exact and the mean is computed from a
+// warp sum; the sum of squared deviations keeps the reference's left-to-right rounding (the
+// terms are computed by all lanes, the accumulation by lane 0).
+__device__ bool burnin_stats(Cell& c, const KParams& P, u32 n) {
   Scalars* sc = c.sc;
   const u32 cap = P.hist_cap;
   if (n == 0) {
-    sc->hist_size = 0;
-    sc->hist_head = 0;
-  } else {
-    u64 sum = 0;  // loop sizes are integers < 2^32: the double sum of the reference is exact
-    for (u32 i = 0; i < n; ++i) sum += pos64(c.fwd[i]) - pos64(c.rev[i]);
-    const double mean = (double)sum / (double)n;
-    double ssd = 0.0;
-    for (u32 i = 0; i < n; ++i) {
-      const double d = (double)(pos64(c.fwd[i]) - pos64(c.rev[i])) - mean;
-      ssd = ssd + (d * d);
+    if (ln() == 0) {
+      sc->hist_size = 0;
+      sc->hist_head = 0;
     }
+    __syncwarp();
+    return false;
+  }
+  u64 part = 0;
+  for (u32 i = ln(); i < n; i += 32) part += pos64(c.fwd[i]) - pos64(c.rev[i]);
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) part += __shfl_xor_sync(FULL, part, d);
+  const double mean = (double)part / (double)n;
+  double* terms = reinterpret_cast<double*>(c.sr);  // sr and sf are adjacent: n doubles
+  for (u32 i = ln(); i < n; i += 32) {
+    const double d = (double)(pos64(c.fwd[i]) - pos64(c.rev[i])) - mean;
+    terms[i] = d * d;
+  }
+  __syncwarp();
+  bool done = false;
+  if (ln() == 0) {
+    double ssd = 0.0;
+    for (u32 i = 0; i < n; ++i) ssd = ssd + terms[i];
     const double sd = sqrt(ssd / (double)n);
     if (sc->hist_size == cap) {
       sc->hist_head = (sc->hist_head + 1) % cap;
@@ -1028,47 +1666,60 @@ __device__ bool burnin_stats_serial(Cell& c, const KParams& P, u32 n) {
     c.havg[slot] = mean;
     c.hcfx[slot] = sd / mean;
     sc->hist_size++;
-  }
-  if (sc->hist_size != cap) return false;
-  const u32 w = P.smooth_w;
-  auto ratio = [&](const double* d) {
-    u64 nd = 0;
-    for (u32 i1 = 1, i2 = w + 1; i2 != cap; ++i1, ++i2) {
-      double a1 = 0.0, a2 = 0.0;
-      for (u32 k = i1 - 1; k < i2 - 1; ++k) a1 = a1 + d[(sc->hist_head + k) % cap];
-      for (u32 k = i1; k < i2; ++k) a2 = a2 + d[(sc->hist_head + k) % cap];
-      const double n1 = a1 / (double)(i2 - i1), n2 = a2 / (double)(i2 - i1);
-      nd += (n1 > n2) ? 1u : 0u;
+    if (sc->hist_size == cap) {
+      const u32 w = P.smooth_w;
+      auto ratio = [&](const double* d) {
+        u64 nd = 0;
+        for (u32 i1 = 1, i2 = w + 1; i2 != cap; ++i1, ++i2) {
+          double a1 = 0.0, a2 = 0.0;
+          for (u32 k = i1 - 1; k < i2 - 1; ++k) a1 = a1 + d[(sc->hist_head + k) % cap];
+          for (u32 k = i1; k < i2; ++k) a2 = a2 + d[(sc->hist_head + k) % cap];
+          const double n1 = a1 / (double)(i2 - i1), n2 = a2 / (double)(i2 - i1);
+          nd += (n1 > n2) ? 1u : 0u;
+        }
+        return (double)nd / (double)((u64)cap - w - nd);
+      };
+      const double r1 = ratio(c.hcfx);
+      if (r1 >= 0.95 && r1 <= 1.05) {
+        const double r2 = ratio(c.havg);
+        done = r2 >= 0.95 && r2 <= 1.05;
+      }
     }
-    return (double)nd / (double)((u64)cap - w - nd);
-  };
-  const double r1 = ratio(c.hcfx);
-  if (!(r1 >= 0.95 && r1 <= 1.05)) return false;
-  const double r2 = ratio(c.havg);
-  return r2 >= 0.95 && r2 <= 1.05;
+    sc->flag = done ? 1u : 0u;
+  }
+  __syncwarp();
+  return sc->flag != 0;
 }
 
-// run_burnin (simulation.cpp:1027-1054); lane 0
-__device__ void run_burnin_serial(Cell& c, const KParams& P) {
+// run_burnin (simulation.cpp:1027-1054)
+__device__ void run_burnin(Cell& c, u64* s, const KParams& P) {
   Scalars* sc = c.sc;
   for (u64 it = 0; it < MGPU_ITER_LIMIT; ++it) {
-    ++sc->num_burnin_epochs;
+    if (ln() == 0) ++sc->num_burnin_epochs;
+    __syncwarp();
     if (sc->num_active != P.nlefs) {
-      const u64 k = s_poisson(c, P);
-      sc->num_active = min(sc->num_active + k, (u64)P.nlefs);
+      rng_ensure(c, s, 64);
+      if (ln() == 0) {
+        const u64 k = s_poisson(c, P);
+        sc->num_active = min(sc->num_active + k, (u64)P.nlefs);
+      }
+      __syncwarp();
     } else {
-      bool done = burnin_stats_serial(c, P, (u32)sc->num_active);
+      bool done = burnin_stats(c, P, (u32)sc->num_active);
       done = done && (sc->epoch > P.min_burnin);
       if (!done && sc->epoch >= P.max_burnin) done = true;
-      sc->burnin_completed = done ? 1 : 0;
+      if (ln() == 0) sc->burnin_completed = done ? 1 : 0;
+      __syncwarp();
     }
     if (sc->num_active != 0) return;
   }
-  set_status(c, DEV_ERR_ITER_LIMIT);
+  if (ln() == 0) set_status(c, DEV_ERR_ITER_LIMIT);
+  __syncwarp();
 }
 
-// ContactMatrixDense::increment (contact_matrix_dense_safe_impl.hpp:52-87)
-__device__ __forceinline__ void band_increment(Cell& c, const KParams& P, u64 row, u64 col) {
+// ContactMatrixDense::increment (contact_matrix_dense_safe_impl.hpp:52-87); returns whether
+// the contact fell outside the band (missed update).
+__device__ __forceinline__ bool band_increment(Cell& c, const KParams& P, u64 row, u64 col) {
   u64 i, j;
   if (row > col) {
     i = row - col;
@@ -1077,20 +1728,205 @@ __device__ __forceinline__ void band_increment(Cell& c, const KParams& P, u64 ro
     i = col - row;
     j = col;
   }
-  if (i >= P.nrows) {
-    c.sc->missed++;
-    return;
-  }
+  if (i >= P.nrows) return true;
   if (c.band) atomicAdd(&c.band[j * P.nrows + i], 1u);
+  return false;
 }
 
-// sample_and_register_contacts (register_contacts.cpp:94-198); lane 0
+__device__ u64 s_uniform_int(Cell& c, u64 a, u64 b);
+__device__ double s_gev(Cell& c, const KParams& P);
+__device__ i64 s_binomial(Cell& c, const KParams& P, i64 t_, double p_);
+__device__ __forceinline__ double canonical_of(u64 u);
+
+// One contact attempt read from draws at `off` (register_contacts.cpp:129-198).  Returns the
+// draws it takes; *ok tells whether it registers a contact; *regular is false when the attempt
+// hit a bucket rejection (exact handling needs the serial path).
+__device__ __forceinline__ u32 contact_attempt(const Cell& c, const KParams& P, u64 off, bool tad,
+                                               u64 na, u64 lbucket, bool* ok, bool* regular,
+                                               u64* row, u64* col) {
+  *ok = false;
+  *regular = true;
+  const u64 start = (u64)P.start + 1, end = (u64)P.end - 1;
+  u32 used = 0;
+  const u64 li = ring_at(c, c.sc->rpos + off + used++) / lbucket;
+  if (li > na - 1) {
+    *regular = false;
+    return used;
+  }
+  if (c.bep[li] == UNBOUND) return used;
+  const u64 rp = pos64(c.rev[li]), fp = pos64(c.fwd[li]);
+  if (!(rp > start && rp < end && fp > start && fp < end)) return used;
+  double n1 = 0.0, n2 = 0.0;
+  if (P.noisify) {
+    const double u1 = canonical_of(ring_at(c, c.sc->rpos + off + used++));
+    n1 = (P.gev_xi == 0.0) ? (P.gev_mu - P.gev_sigma) * log(-log(u1))
+                           : P.gev_mu + (P.gev_sigma * (1.0 - pow(-log(u1), P.gev_xi))) / P.gev_xi;
+  }
+  const double a = (double)rp - n1;
+  if (P.noisify) {
+    const double u2 = canonical_of(ring_at(c, c.sc->rpos + off + used++));
+    n2 = (P.gev_xi == 0.0) ? (P.gev_mu - P.gev_sigma) * log(-log(u2))
+                           : P.gev_mu + (P.gev_sigma * (1.0 - pow(-log(u2), P.gev_xi))) / P.gev_xi;
+  }
+  const double b = (double)fp + n2;
+  const double p1 = fmin(a, b), p2 = fmax(a, b);
+  const double ds = (double)start, de = (double)end;
+  if (!(p1 >= ds && p2 >= ds && p1 < de && p2 < de)) return used;
+  if (!tad) {
+    *row = ((u64)p1 - start) / P.bin;
+    *col = ((u64)p2 - start) / P.bin;
+    *ok = true;
+    return used;
+  }
+  const u64 q1 = (u64)p1, q2 = (u64)p2;
+  const u64 range = q2 - q1;
+  u64 p11 = q1, p22 = q1;
+  if (range != 0) {
+    u64 bucket = ~0ull / (range + 1);
+    if (~0ull % (range + 1) == range) ++bucket;
+    const u64 r1 = ring_at(c, c.sc->rpos + off + used++) / bucket;
+    if (r1 > range) {
+      *regular = false;
+      return used;
+    }
+    const u64 r2 = ring_at(c, c.sc->rpos + off + used++) / bucket;
+    if (r2 > range) {
+      *regular = false;
+      return used;
+    }
+    p11 = q1 + r1;
+    p22 = q1 + r2;
+  }
+  *row = (p11 - start) / P.bin;
+  *col = (p22 - start) / P.bin;
+  *ok = true;
+  return used;
+}
+
+// Lane 0: one contact attempt with serial draws (the exact path for rejections).
+__device__ void contact_attempt_serial(Cell& c, const KParams& P, bool tad, u64 na, bool* ok, bool* miss) {
+  *ok = false;
+  *miss = false;
+  const u64 start = (u64)P.start + 1, end = (u64)P.end - 1;
+  const u64 li = s_uniform_int(c, 0, na - 1);
+  if (c.bep[li] == UNBOUND) return;
+  const u64 rp = pos64(c.rev[li]), fp = pos64(c.fwd[li]);
+  if (!(rp > start && rp < end && fp > start && fp < end)) return;
+  const double n1 = P.noisify ? s_gev(c, P) : 0.0;
+  const double a = (double)rp - n1;
+  const double n2 = P.noisify ? s_gev(c, P) : 0.0;
+  const double b = (double)fp + n2;
+  const double p1 = fmin(a, b), p2 = fmax(a, b);
+  if (!(p1 >= (double)start && p2 >= (double)start && p1 < (double)end && p2 < (double)end)) return;
+  if (!tad) {
+    *miss = band_increment(c, P, ((u64)p1 - start) / P.bin, ((u64)p2 - start) / P.bin);
+  } else {
+    const u64 p11 = s_uniform_int(c, (u64)p1, (u64)p2);
+    const u64 p22 = s_uniform_int(c, (u64)p1, (u64)p2);
+    *miss = band_increment(c, P, (p11 - start) / P.bin, (p22 - start) / P.bin);
+  }
+  *ok = true;
+}
+
+// sample_and_register_contacts (register_contacts.cpp:94-198): attempts are evaluated 32 at a
+// time at the offsets they would have if each took the usual number of draws (1 for the LEF,
+// 2 for the noise, 2 more for a TAD contact).  The warp commits up to the first attempt that
+// took a different number (a LEF or position outside the bounds, a zero-width TAD range) and
+// resumes after it; an attempt that hit a uniform_int bucket rejection is redone serially.
+__device__ void sample_contacts(Cell& c, u64* s, const KParams& P, u64 target) {
+  Scalars* sc = c.sc;
+  u64 num = P.spe;
+  if (P.density_positive) num = min(num, target - sc->num_contacts);
+  if (num == 0) return;
+  rng_ensure(c, s, 64);
+  if (ln() == 0) {
+    u64 n_loop;
+    if (P.ratio_mode == 0) {
+      n_loop = num;
+    } else if (P.ratio_mode == 1) {
+      n_loop = 0;
+    } else {
+      n_loop = (u64)s_binomial(c, P, (i64)num, P.p_loop);
+    }
+    sc->bc0 = n_loop;
+  }
+  __syncwarp();
+  const u64 n_loop = sc->bc0;
+  const u64 na = sc->num_active;
+  u64 lbucket;
+  {
+    const u64 range = na - 1;
+    lbucket = ~0ull / (range + 1);
+    if (~0ull % (range + 1) == range) ++lbucket;
+  }
+  const bool serial = P.debug_flags & DBG_SERIAL_CONTACTS;
+  u64 budget = 1000 * num + 1000000;  // attempts before giving up (see DEV_ERR_NO_BOUND_LEF)
+  u32 missed = 0;
+  for (int pass = 0; pass < 2; ++pass) {
+    const bool tad = pass == 1;
+    u64 todo = tad ? num - n_loop : n_loop;
+    const u32 nominal = 1 + (P.noisify ? 2 : 0) + (tad ? 2 : 0);
+    while (todo != 0) {
+      if (budget < 32) {
+        if (ln() == 0) set_status(c, DEV_ERR_NO_BOUND_LEF);
+        __syncwarp();
+        return;
+      }
+      budget -= 32;
+      rng_ensure(c, s, 32 * 5);
+      bool ok = false, regular = true;
+      u64 row = 0, col = 0;
+      u32 used = nominal;
+      if (!serial) used = contact_attempt(c, P, (u64)ln() * nominal, tad, na, lbucket, &ok, &regular, &row, &col);
+      const bool deviates = serial || !regular || used != nominal;
+      const unsigned dm = __ballot_sync(FULL, deviates);
+      const u32 f = dm ? (u32)(__ffs(dm) - 1) : 32u;
+      const bool f_regular = f < 32 && __shfl_sync(FULL, regular && !serial, f);
+      u32 lim = (f == 32) ? 32u : (f_regular ? f + 1 : f);  // lanes [0, lim) are exact
+      const unsigned okm = __ballot_sync(FULL, ok && ln() < lim);
+      if ((u64)__popc(okm) >= todo) {  // the todo-th success ends the pass
+        unsigned mm = okm;
+        for (u64 t = 1; t < todo; ++t) mm &= mm - 1;
+        lim = (u32)__ffs(mm);
+      }
+      const unsigned lanes = lim >= 32 ? FULL : ((1u << lim) - 1);
+      if (ok && ((lanes >> ln()) & 1u) && band_increment(c, P, row, col)) ++missed;
+      const u32 draws = lim == 0 ? 0 : (lim - 1) * nominal + __shfl_sync(FULL, used, lim == 0 ? 0 : lim - 1);
+      todo -= __popc(okm & lanes);
+      __syncwarp();
+      if (ln() == 0) sc->rpos += draws;
+      __syncwarp();
+      if (todo != 0 && lim == f && f < 32) {
+        // attempt f could not be evaluated from the ring: run it serially
+        if (ln() == 0) {
+          bool sok, smiss;
+          contact_attempt_serial(c, P, tad, na, &sok, &smiss);
+          sc->bc1 = sok ? 1 : 0;
+          if (smiss) sc->missed++;
+        }
+        __syncwarp();
+        if (sc->bc1) todo -= 1;
+        __syncwarp();
+        if (sc->status != DEV_OK) return;
+      }
+    }
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) missed += __shfl_xor_sync(FULL, missed, d);
+  if (ln() == 0) {
+    sc->missed += missed;
+    sc->num_contacts += num;
+  }
+  __syncwarp();
+}
+
+// sample_and_register_contacts with serial draws (lane 0): the exact path behind the
+// DBG_SERIAL_CONTACTS switch.
 __device__ void sample_contacts_serial(Cell& c, const KParams& P, u64 target) {
   Scalars* sc = c.sc;
   u64 num = P.spe;
   if (P.density_positive) num = min(num, target - sc->num_contacts);
   if (num == 0) return;
-  const u64 start = (u64)P.start + 1, end = (u64)P.end - 1;
   u64 n_loop;
   if (P.ratio_mode == 0) {
     n_loop = num;
@@ -1099,45 +1935,26 @@ __device__ void sample_contacts_serial(Cell& c, const KParams& P, u64 target) {
   } else {
     n_loop = (u64)s_binomial(c, P, (i64)num, P.p_loop);
   }
-  const u64 n_tad = num - n_loop;
-  const double ds = (double)start, de = (double)end;
-  const u64 na = sc->num_active;
-  // attempts budget: rejections are rare in a valid run (units at the chromosome ends, noise
-  // outside the range); a chromosome where no LEF can register a contact ends with an error
-  // instead of looping forever
   u64 budget = 1000 * num + 1000000;
   for (int pass = 0; pass < 2; ++pass) {
-    u64 todo = pass == 0 ? n_loop : n_tad;
+    u64 todo = pass == 0 ? n_loop : num - n_loop;
     while (todo != 0) {
       if (--budget == 0 || sc->status != DEV_OK) {
         set_status(c, DEV_ERR_NO_BOUND_LEF);
         return;
       }
-      const u64 li = s_uniform_int(c, 0, na - 1);
-      if (c.bep[li] == UNBOUND) continue;
-      const u64 rp = pos64(c.rev[li]), fp = pos64(c.fwd[li]);
-      if (!(rp > start && rp < end && fp > start && fp < end)) continue;
-      const double n1 = P.noisify ? s_gev(c, P) : 0.0;
-      const double a = (double)rp - n1;
-      const double n2 = P.noisify ? s_gev(c, P) : 0.0;
-      const double b = (double)fp + n2;
-      const double p1 = fmin(a, b), p2 = fmax(a, b);
-      if (!(p1 >= ds && p2 >= ds && p1 < de && p2 < de)) continue;
-      if (pass == 0) {
-        band_increment(c, P, ((u64)p1 - start) / P.bin, ((u64)p2 - start) / P.bin);
-      } else {
-        const u64 q1 = (u64)p1, q2 = (u64)p2;
-        const u64 p11 = s_uniform_int(c, q1, q2);
-        const u64 p22 = s_uniform_int(c, q1, q2);
-        band_increment(c, P, (p11 - start) / P.bin, (p22 - start) / P.bin);
-      }
-      --todo;
+      bool ok, miss;
+      contact_attempt_serial(c, P, pass == 1, sc->num_active, &ok, &miss);
+      if (miss) sc->missed++;
+      if (ok) --todo;
     }
   }
   sc->num_contacts += num;
 }
 
-// mgpu_state_digest / trace record of one epoch: warp-parallel.
+// ---------------------------------------------------------------------------------------
+// Trace, cell setup and the epoch loop (simulation.cpp:1056-1152)
+// ---------------------------------------------------------------------------------------
 __device__ __forceinline__ u64 mix64(u64 z) {
   z ^= z >> 30;
   z *= 0xbf58476d1ce4e5b9ull;
@@ -1147,11 +1964,12 @@ __device__ __forceinline__ u64 mix64(u64 z) {
   return z;
 }
 
+// mgpu_state_digest of the cell's state, and the full arrays when requested.
 __device__ void trace_record(Cell& c, const KParams& P, const DevTrace& T, u64 rec) {
   const u32 nl = P.nlefs;
   const bool full = rec < T.max_records;
   u64 part = 0;
-  for (u32 i = c.lane; i < nl; i += 32) {
+  for (u32 i = ln(); i < nl; i += 32) {
     const u64 v[9] = {pos64(c.rev[i]), pos64(c.fwd[i]), pos64(c.bep[i]), c.rr[i], c.fr[i],
                       c.rm[i], c.fm[i], cw_to_ref(c.rc[i]), cw_to_ref(c.fc[i])};
     u64 h = mix64((u64)i * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull);
@@ -1170,8 +1988,9 @@ __device__ void trace_record(Cell& c, const KParams& P, const DevTrace& T, u64 r
       if (T.fwd_collision) T.fwd_collision[o] = v[8];
     }
   }
-  for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, off);
-  if (c.lane == 0) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(FULL, part, off);
+  if (ln() == 0) {
     const Scalars* sc = c.sc;
     mgpu_trace_header h;
     h.epoch = sc->epoch;
@@ -1189,36 +2008,37 @@ __device__ void trace_record(Cell& c, const KParams& P, const DevTrace& T, u64 r
   __syncwarp();
 }
 
-// ---------------------------------------------------------------------------------------
-// Cell setup and the epoch loop (simulation.cpp:1056-1152)
-// ---------------------------------------------------------------------------------------
-__device__ void carve(Cell& c, char* smem, const KParams& P, u32 nl) {
-  char* p = smem;
-  c.sc = reinterpret_cast<Scalars*>(p);
-  p += 512;
-  c.ring = reinterpret_cast<u64*>(p);
-  p += (u64)RING * 8;
-  c.hcfx = reinterpret_cast<double*>(p);
-  p += (u64)P.hist_cap * 8;
-  c.havg = reinterpret_cast<double*>(p);
-  p += (u64)P.hist_cap * 8;
-  c.bst = reinterpret_cast<u32*>(p);
-  p += ((((u64)c.nb + 31) / 32) * 4 + 15) & ~15ull;
-  u32* a = reinterpret_cast<u32*>(p);
-  c.rev = a;
-  c.fwd = a + nl;
-  c.bep = a + 2 * (u64)nl;
-  c.rr = a + 3 * (u64)nl;
-  c.fr = a + 4 * (u64)nl;
-  c.rm = a + 5 * (u64)nl;
-  c.fm = a + 6 * (u64)nl;
-  c.rc = a + 7 * (u64)nl;
-  c.fc = a + 8 * (u64)nl;
-  c.tmp = a + 9 * (u64)nl;
+// Lay out one cell: the header in shared memory, then each per-LEF array either in shared
+// memory or in the block's global scratch slot, as planned by the host.
+__device__ void carve(Cell& c, char* smem, char* gslot, const KParams& P, u32 nl, const DevChrom& ch,
+                      const ulonglong2* jt, u32* band) {
+  if (ln() == 0) {
+    char* p = smem;
+    c.sc = reinterpret_cast<Scalars*>(p);
+    p += CELL_HEADER_BYTES;
+    c.ring = reinterpret_cast<u64*>(p);
+    p += (u64)RING * 8;
+    c.hcfx = reinterpret_cast<double*>(p);
+    p += (u64)P.hist_cap * 8;
+    c.havg = reinterpret_cast<double*>(p);
+    p += (u64)P.hist_cap * 8;
+    c.bst = reinterpret_cast<u32*>(p);
+    u32** arr[NARR] = {&c.rev, &c.fwd, &c.rr, &c.fr, &c.rm, &c.fm, &c.rc, &c.fc, &c.sr, &c.sf, &c.tmp, &c.bep};
+    for (u32 k = 0; k < NARR; ++k) {
+      char* base = ((P.arr_smem >> k) & 1u) ? smem : gslot;
+      *arr[k] = reinterpret_cast<u32*>(base + P.arr_off[k]);
+    }
+    c.bar = ch.barriers;
+    c.nb = ch.nbarriers;
+    c.nl = nl;
+    c.jt = jt;
+    c.band = band;
+  }
+  __syncwarp();
 }
 
 __device__ void cell_reset(Cell& c, u32 nl, u64 seed) {
-  for (u32 i = c.lane; i < nl; i += 32) {
+  for (u32 i = ln(); i < nl; i += 32) {
     c.rev[i] = UNBOUND;
     c.fwd[i] = UNBOUND;
     c.bep[i] = UNBOUND;
@@ -1229,8 +2049,8 @@ __device__ void cell_reset(Cell& c, u32 nl, u64 seed) {
     c.rc[i] = 0;
     c.fc[i] = 0;
   }
-  for (u32 w = c.lane; w < (c.nb + 31) / 32; w += 32) c.bst[w] = 0;
-  if (c.lane == 0) {
+  for (u32 w = ln(); w < (c.nb + 31) / 32; w += 32) c.bst[w] = 0;
+  if (ln() == 0) {
     Scalars* sc = c.sc;
     u64 st = seed;  // SplitMix64 seeding (random.hpp:26-30)
     for (int k = 0; k < 4; ++k) {
@@ -1254,18 +2074,19 @@ __device__ void cell_reset(Cell& c, u32 nl, u64 seed) {
     sc->n5 = sc->n3 = 0;
     sc->hist_size = 0;
     sc->hist_head = 0;
-    sc->records = 0;
+    sc->bc0 = sc->bc1 = sc->bc2 = 0;
+    sc->flag = 0;
   }
   __syncwarp();
 }
 
-__device__ void run_cell(Cell& c, const KParams& P, const CellTask& task, u64 target_epochs,
+__device__ void run_cell(Cell& c, u64* s, const KParams& P, const CellTask& task, u64 target_epochs,
                          const DevTrace* trace, mgpu_cell_stats* stats) {
   Scalars* sc = c.sc;
   const u32 nl = P.nlefs;
   cell_reset(c, nl, task.seed);
-  barriers_init(c);
-  if (P.skip_burnin && c.lane == 0) {
+  barriers_init(c, s);
+  if (P.skip_burnin && ln() == 0) {
     sc->num_active = nl;
     sc->burnin_completed = 1;
   }
@@ -1275,62 +2096,44 @@ __device__ void run_cell(Cell& c, const KParams& P, const CellTask& task, u64 ta
     const bool go = P.contact_mode ? (sc->num_contacts < target)
                                    : (sc->epoch - sc->num_burnin_epochs < target_epochs);
     if (!go) break;
-    if (!sc->burnin_completed) {
-      rng_ensure(c, RNG_BLOCK);
-      if (c.lane == 0) run_burnin_serial(c, P);
-      __syncwarp();
-    }
+    if (!sc->burnin_completed) run_burnin(c, s, P);
     const u32 n = (u32)sc->num_active;
     const u32 epoch = (u32)sc->epoch;
     const bool completed = sc->burnin_completed != 0;
-    if (c.lane == 0) sc->lef_epochs += n;
-    bind_lefs(c, P, n, epoch, 0, nullptr);
-    if (c.lane == 0) rank_lefs_serial(c, n, epoch != 0, false);
-    __syncwarp();
+    if (ln() == 0) sc->lef_epochs += n;
+    bind_lefs(c, s, P, n, epoch, 0, nullptr);
+    rank_lefs(c, P, n, epoch, epoch != 0);
     if (completed) {
-      rng_ensure(c, RNG_BLOCK);
-      if (c.lane == 0) sample_contacts_serial(c, P, target);
-      __syncwarp();
+      if (P.debug_flags & DBG_SERIAL_CONTACTS) {
+        rng_ensure(c, s, RNG_BLOCK);
+        if (ln() == 0) sample_contacts_serial(c, P, target);
+        __syncwarp();
+      } else {
+        sample_contacts(c, s, P, target);
+      }
       if (target != 0 && sc->num_contacts >= target) break;
       if (sc->status != DEV_OK) break;
     }
-    gen_moves_dir(c, c.rm, n, P.rev_speed[completed], P.rev_std, P.rev_move_int[completed]);
-    gen_moves_dir(c, c.fm, n, P.fwd_speed[completed], P.fwd_std, P.fwd_move_int[completed]);
-    if (c.lane == 0) adjust_moves_serial(c, P, n);
-    __syncwarp();
+    gen_moves_dir(c, s, c.rm, n, P.rev_speed[completed], P.rev_std, P.rev_move_int[completed]);
+    gen_moves_dir(c, s, c.fm, n, P.fwd_speed[completed], P.fwd_std, P.fwd_move_int[completed]);
+    gather_ranked(c, n);
+    adjust_moves(c, P, n);
     clamp_moves(c, P, n);
-    barriers_next(c);
-    for (u32 i = c.lane; i < n; i += 32) {
+    barriers_next(c, s);
+    for (u32 i = ln(); i < n; i += 32) {
       c.rc[i] = 0;
       c.fc[i] = 0;
     }
     __syncwarp();
-    rng_ensure(c, RNG_BLOCK);
-    if (c.lane == 0) {
-      u64 n5, n3;
-      detect_boundaries_serial(c, P, n, n5, n3);
-      detect_lef_bar_serial(c, P, n, n5, n3);
-      detect_primary_serial(c, P, n, n5, n3);
-      sc->n5 = n5;
-      sc->n3 = n3;
-    }
-    __syncwarp();
-    correct_lef_bar(c, n);
-    correct_primary(c, n);
-    rng_ensure(c, RNG_BLOCK);
-    if (c.lane == 0) {
-      process_secondary_serial(c, P, n, sc->n5, sc->n3);
-      fix_secondary_serial(c, P, n, sc->n5, sc->n3);
-    }
-    __syncwarp();
+    process_collisions(c, s, P, n, true);
     extrude(c, n);
-    release_lefs(c, P, n, completed);
+    release_lefs(c, s, P, n, completed);
     if (trace) trace_record(c, P, *trace, sc->epoch);
-    if (c.lane == 0) sc->epoch++;
+    if (ln() == 0) sc->epoch++;
     __syncwarp();
     if (sc->status != DEV_OK) break;
   }
-  if (c.lane == 0) {
+  if (ln() == 0) {
     if (trace && trace->num_recorded) *trace->num_recorded = sc->epoch;
     if (stats) {
       stats->epochs = sc->epoch;
@@ -1350,24 +2153,19 @@ __global__ void __launch_bounds__(32) simulate_kernel(const __grid_constant__ KP
                                                       const CellTask* tasks, u64 ncells,
                                                       u64 target_epochs, u32* band, u64* missed,
                                                       mgpu_cell_stats* stats, DevTrace trace,
-                                                      u32 tracing, const ulonglong2* jt,
-                                                      u32* work) {
+                                                      u32 tracing, const ulonglong2* jt, u32* work,
+                                                      char* gscratch) {
   extern __shared__ __align__(16) char smem[];
-  Cell c;
-  c.lane = threadIdx.x & 31;
-  c.bar = ch.barriers;
-  c.nb = ch.nbarriers;
-  c.jt = jt;
-  c.band = band;
-  carve(c, smem, P, P.nlefs);
+  __shared__ Cell c;
+  u64 s[4] = {0, 0, 0, 0};
+  carve(c, smem, gscratch + (u64)blockIdx.x * P.slot_bytes, P, P.nlefs, ch, jt, band);
   for (;;) {
     u32 cell = 0;
-    if (c.lane == 0) cell = atomicAdd(work, 1u);
-    cell = __shfl_sync(0xFFFFFFFFu, cell, 0);
+    if (ln() == 0) cell = atomicAdd(work, 1u);
+    cell = __shfl_sync(FULL, cell, 0);
     if (cell >= ncells) break;
-    run_cell(c, P, tasks[cell], target_epochs, tracing ? &trace : nullptr,
-             stats ? stats + cell : nullptr);
-    if (c.lane == 0 && missed) atomicAdd((unsigned long long*)missed, (unsigned long long)c.sc->missed);
+    run_cell(c, s, P, tasks[cell], target_epochs, tracing ? &trace : nullptr, stats ? stats + cell : nullptr);
+    if (ln() == 0 && missed) atomicAdd((unsigned long long*)missed, (unsigned long long)c.sc->missed);
     __syncwarp();
   }
 }
@@ -1378,18 +2176,14 @@ __global__ void __launch_bounds__(32) phase_kernel(const __grid_constant__ KPara
                                                    uint8_t* barrier_state, u64 epoch,
                                                    u32 burnin_completed, u32 partially_sorted,
                                                    u32 init_ranks, u32 adjust, u64* prng,
-                                                   u64* outs, const ulonglong2* jt) {
+                                                   u64* outs, const ulonglong2* jt, char* gslot) {
   extern __shared__ __align__(16) char smem[];
-  Cell c;
-  c.lane = threadIdx.x & 31;
-  c.bar = ch.barriers;
-  c.nb = ch.nbarriers;
-  c.jt = jt;
-  c.band = nullptr;
-  carve(c, smem, P, n);
+  __shared__ Cell c;
+  u64 s[4] = {0, 0, 0, 0};
+  carve(c, smem, gslot, P, n, ch, jt, nullptr);
   u64* A[9];
   for (int k = 0; k < 9; ++k) A[k] = arrays + (u64)k * n;
-  for (u32 i = c.lane; i < n; i += 32) {
+  for (u32 i = ln(); i < n; i += 32) {
     c.rev[i] = A[0][i] == ~0ull ? UNBOUND : (u32)A[0][i];
     c.fwd[i] = A[1][i] == ~0ull ? UNBOUND : (u32)A[1][i];
     c.bep[i] = A[2][i] == ~0ull ? UNBOUND : (u32)A[2][i];
@@ -1400,7 +2194,7 @@ __global__ void __launch_bounds__(32) phase_kernel(const __grid_constant__ KPara
     c.rc[i] = cw_from_ref(A[7][i]);
     c.fc[i] = cw_from_ref(A[8][i]);
   }
-  for (u32 w = c.lane; w < (c.nb + 31) / 32; w += 32) {
+  for (u32 w = ln(); w < (c.nb + 31) / 32; w += 32) {
     u32 bits = 0;
     for (u32 b = 0; b < 32; ++b) {
       const u32 i = w * 32 + b;
@@ -1410,7 +2204,7 @@ __global__ void __launch_bounds__(32) phase_kernel(const __grid_constant__ KPara
   }
   u64 init_state[4];
   for (int k = 0; k < 4; ++k) init_state[k] = prng[k];
-  if (c.lane == 0) {
+  if (ln() == 0) {
     Scalars* sc = c.sc;
     for (int k = 0; k < 4; ++k) sc->canon[k] = prng[k];
     sc->rpos = sc->gpos = 0;
@@ -1419,70 +2213,87 @@ __global__ void __launch_bounds__(32) phase_kernel(const __grid_constant__ KPara
     sc->epoch = epoch;
     sc->num_active = n;
     sc->burnin_completed = burnin_completed;
+    sc->sort_fallbacks = 0;
   }
   __syncwarp();
   const bool completed = burnin_completed != 0;
-  u64 n5 = 0, n3 = 0, released = 0;
+  u64 released = 0;
   switch (phase) {
     case MGPU_PHASE_BIND:
-      bind_lefs(c, P, n, (u32)epoch, bind_mask ? 1 : 2, bind_mask);
-      if (c.lane == 0) rank_lefs_serial(c, n, epoch != 0, false);
+      bind_lefs(c, s, P, n, (u32)epoch, bind_mask ? 1 : 2, bind_mask);
+      rank_lefs(c, P, n, (u32)epoch, epoch != 0);
       break;
     case MGPU_PHASE_RANK:
-      if (c.lane == 0) rank_lefs_serial(c, n, partially_sorted != 0, init_ranks != 0);
+      if (init_ranks) {
+        for (u32 i = ln(); i < n; i += 32) {
+          c.rr[i] = i;
+          c.fr[i] = i;
+        }
+        __syncwarp();
+      }
+      rank_lefs(c, P, n, (u32)epoch, partially_sorted != 0);
       break;
     case MGPU_PHASE_ADJUST_AND_CLAMP:
-      if (c.lane == 0) adjust_moves_serial(c, P, n);
-      __syncwarp();
+      gather_ranked(c, n);
+      adjust_moves(c, P, n);
       clamp_moves(c, P, n);
       break;
     case MGPU_PHASE_GENERATE_MOVES:
-      gen_moves_dir(c, c.rm, n, P.rev_speed[completed], P.rev_std, P.rev_move_int[completed]);
-      gen_moves_dir(c, c.fm, n, P.fwd_speed[completed], P.fwd_std, P.fwd_move_int[completed]);
-      if (adjust && c.lane == 0) adjust_moves_serial(c, P, n);
-      __syncwarp();
+      gen_moves_dir(c, s, c.rm, n, P.rev_speed[completed], P.rev_std, P.rev_move_int[completed]);
+      gen_moves_dir(c, s, c.fm, n, P.fwd_speed[completed], P.fwd_std, P.fwd_move_int[completed]);
+      if (adjust) {
+        gather_ranked(c, n);
+        adjust_moves(c, P, n);
+      }
       clamp_moves(c, P, n);
       break;
     case MGPU_PHASE_PROCESS_COLLISIONS:
-      rng_ensure(c, RNG_BLOCK);
-      if (c.lane == 0) {
-        detect_boundaries_serial(c, P, n, n5, n3);
-        detect_lef_bar_serial(c, P, n, n5, n3);
-        detect_primary_serial(c, P, n, n5, n3);
-        c.sc->n5 = n5;
-        c.sc->n3 = n3;
-      }
-      __syncwarp();
-      correct_lef_bar(c, n);
-      correct_primary(c, n);
-      if (c.lane == 0) process_secondary_serial(c, P, n, c.sc->n5, c.sc->n3);
-      n5 = c.sc->n5;
-      n3 = c.sc->n3;
+      gather_ranked(c, n);
+      process_collisions(c, s, P, n, false);
       break;
     case MGPU_PHASE_FIX_SECONDARY:
-      if (c.lane == 0) fix_secondary_serial(c, P, n, 0, 0);
+      if (ln() == 0) fix_secondary_serial(c, P, n, 0, 0);
       break;
     case MGPU_PHASE_DETECT_LEF_BAR:
-      if (c.lane == 0) detect_lef_bar_serial(c, P, n, 0, 0);
+      gather_ranked(c, n);
+      if (ranked_sorted(c, n) && !(P.debug_flags & DBG_SERIAL_COLLISIONS)) {
+        detect_lef_bar_fast(c, s, P, n, 0, 0);
+      } else {
+        rng_ensure(c, s, RNG_BLOCK);
+        if (ln() == 0) detect_lef_bar_serial(c, P, n, 0, 0);
+      }
       break;
     case MGPU_PHASE_LEF_LEF:
-      if (c.lane == 0) detect_primary_serial(c, P, n, 0, 0);
-      __syncwarp();
-      correct_primary(c, n);
-      if (c.lane == 0) process_secondary_serial(c, P, n, 0, 0);
+      gather_ranked(c, n);
+      if (ranked_sorted(c, n) && !(P.debug_flags & DBG_SERIAL_COLLISIONS)) {
+        detect_primary_fast(c, s, P, n, 0, 0);
+        correct_primary(c, n);
+        secondary_dir_fast(c, s, P, 0, n, 0, 0);
+        secondary_dir_fast(c, s, P, 1, n, 0, 0);
+      } else {
+        rng_ensure(c, s, RNG_BLOCK);
+        if (ln() == 0) detect_primary_serial(c, P, n, 0, 0);
+        __syncwarp();
+        correct_primary(c, n);
+        if (ln() == 0) process_secondary_serial(c, P, n, 0, 0);
+      }
       break;
     case MGPU_PHASE_DETECT_PRIMARY:
-      if (c.lane == 0) detect_primary_serial(c, P, n, 0, 0);
+      gather_ranked(c, n);
+      if (ranked_sorted(c, n) && !(P.debug_flags & DBG_SERIAL_COLLISIONS)) {
+        detect_primary_fast(c, s, P, n, 0, 0);
+      } else {
+        rng_ensure(c, s, RNG_BLOCK);
+        if (ln() == 0) detect_primary_serial(c, P, n, 0, 0);
+      }
       break;
     case MGPU_PHASE_DETECT_BOUNDARIES:
-      if (c.lane == 0) {
+      if (ln() == 0) {
+        u64 n5, n3;
         detect_boundaries_serial(c, P, n, n5, n3);
         c.sc->n5 = n5;
         c.sc->n3 = n3;
       }
-      __syncwarp();
-      n5 = c.sc->n5;
-      n3 = c.sc->n3;
       break;
     case MGPU_PHASE_CORRECT_LEF_BAR:
       correct_lef_bar(c, n);
@@ -1494,19 +2305,19 @@ __global__ void __launch_bounds__(32) phase_kernel(const __grid_constant__ KPara
       extrude(c, n);
       break;
     case MGPU_PHASE_RELEASE:
-      released = release_lefs(c, P, n, completed);
+      released = release_lefs(c, s, P, n, completed);
       break;
     case MGPU_PHASE_BARRIER_NEXT:
-      barriers_next(c);
+      barriers_next(c, s);
       break;
     case MGPU_PHASE_BARRIER_INIT:
-      barriers_init(c);
+      barriers_init(c, s);
       break;
     default:
       break;
   }
   __syncwarp();
-  for (u32 i = c.lane; i < n; i += 32) {
+  for (u32 i = ln(); i < n; i += 32) {
     A[0][i] = pos64(c.rev[i]);
     A[1][i] = pos64(c.fwd[i]);
     A[2][i] = pos64(c.bep[i]);
@@ -1517,16 +2328,16 @@ __global__ void __launch_bounds__(32) phase_kernel(const __grid_constant__ KPara
     A[7][i] = cw_to_ref(c.rc[i]);
     A[8][i] = cw_to_ref(c.fc[i]);
   }
-  for (u32 i = c.lane; i < c.nb; i += 32) {
+  for (u32 i = ln(); i < c.nb; i += 32) {
     if (barrier_state) barrier_state[i] = bar_active(c, i) ? 1 : 0;
   }
-  if (c.lane == 0) {
+  if (ln() == 0) {
     // the caller's PRNG advanced by exactly the number of draws consumed
-    u64 s[4] = {init_state[0], init_state[1], init_state[2], init_state[3]};
-    for (u64 k = 0; k < c.sc->rpos; ++k) xo_next(s);
-    for (int k = 0; k < 4; ++k) prng[k] = s[k];
-    outs[0] = n5;
-    outs[1] = n3;
+    u64 st[4] = {init_state[0], init_state[1], init_state[2], init_state[3]};
+    for (u64 k = 0; k < c.sc->rpos; ++k) xo_next(st);
+    for (int k = 0; k < 4; ++k) prng[k] = st[k];
+    outs[0] = c.sc->n5;
+    outs[1] = c.sc->n3;
     outs[2] = released;
     outs[3] = c.sc->status;
   }
@@ -1548,25 +2359,39 @@ u64 max_smem_per_block() {
   return (u64)v;
 }
 
-int launch_simulate(const KParams& P, const DevChrom& ch, const CellTask* tasks, u64 ncells,
-                    u64 target_epochs, u32* band, u64* missed, mgpu_cell_stats* stats,
-                    const DevTrace* trace, const void* jump_table, u32* work_counter,
-                    void* stream, char* errbuf, int errlen) {
-  const u64 smem = cell_smem_bytes(P.nlefs, ch.nbarriers, P.hist_cap);
-  int rc = cuda_fail(cudaFuncSetAttribute(simulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem),
-                     "cudaFuncSetAttribute", errbuf, errlen);
-  if (rc) return rc;
+u64 resident_cells(const KParams& P, u64 ncells) {
+  if (cudaFuncSetAttribute(simulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem_bytes) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
   int per_sm = 0;
-  rc = cuda_fail(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, simulate_kernel, 32, smem),
-                 "occupancy", errbuf, errlen);
-  if (rc) return rc;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, simulate_kernel, 32, P.smem_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   u64 grid = (u64)sms * (u64)(per_sm > 0 ? per_sm : 1);
-  if (grid > ncells) grid = ncells;
+  return grid < ncells ? grid : ncells;
+}
+
+int launch_simulate(const KParams& P, const DevChrom& ch, const CellTask* tasks, u64 ncells,
+                    u64 target_epochs, u32* band, u64* missed, mgpu_cell_stats* stats,
+                    const DevTrace* trace, const void* jump_table, u32* work_counter,
+                    char* gscratch, u64 gscratch_bytes, void* stream, char* errbuf, int errlen) {
+  int rc = cuda_fail(cudaFuncSetAttribute(simulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)P.smem_bytes),
+                     "cudaFuncSetAttribute", errbuf, errlen);
+  if (rc) return rc;
+  u64 grid = resident_cells(P, ncells);
   if (grid == 0) return MGPU_OK;
+  if (P.slot_bytes && gscratch_bytes / P.slot_bytes < grid) grid = gscratch_bytes / P.slot_bytes;
+  if (grid == 0) {
+    if (errbuf) snprintf(errbuf, errlen, "global scratch too small for one cell");
+    return MGPU_ERR_INTERNAL;
+  }
   cudaStream_t st = (cudaStream_t)stream;
   rc = cuda_fail(cudaMemsetAsync(work_counter, 0, sizeof(u32), st), "memset", errbuf, errlen);
   if (rc) return rc;
@@ -1576,26 +2401,25 @@ int launch_simulate(const KParams& P, const DevChrom& ch, const CellTask* tasks,
     tr = *trace;
     tracing = 1;
   }
-  simulate_kernel<<<(unsigned)grid, 32, smem, st>>>(P, ch, tasks, ncells, target_epochs, band,
-                                                    missed, stats,
-                                                    tr, tracing,
-                                                    (const ulonglong2*)jump_table, work_counter);
+  simulate_kernel<<<(unsigned)grid, 32, P.smem_bytes, st>>>(P, ch, tasks, ncells, target_epochs, band,
+                                                             missed, stats, tr, tracing,
+                                                             (const ulonglong2*)jump_table, work_counter,
+                                                             gscratch);
   return cuda_fail(cudaGetLastError(), "simulate_kernel launch", errbuf, errlen);
 }
 
 int launch_phase(const KParams& P, const DevChrom& ch, int phase, u64 n, u64* arrays,
                  u64* bind_mask, uint8_t* barrier_state, u64 epoch, u32 burnin_completed,
                  u32 partially_sorted, u32 init_ranks, u32 adjust, u64* prng_state, u64* outs,
-                 const void* jump_table, void* stream, char* errbuf, int errlen) {
-  const u64 smem = cell_smem_bytes(n, ch.nbarriers, P.hist_cap);
+                 const void* jump_table, char* gscratch, void* stream, char* errbuf, int errlen) {
   int rc = cuda_fail(cudaFuncSetAttribute(phase_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem),
+                                          (int)P.smem_bytes),
                      "cudaFuncSetAttribute", errbuf, errlen);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
-  phase_kernel<<<1, 32, smem, st>>>(P, ch, phase, (u32)n, arrays, bind_mask, barrier_state,
-                                     epoch, burnin_completed, partially_sorted, init_ranks, adjust,
-                                     prng_state, outs, (const ulonglong2*)jump_table);
+  phase_kernel<<<1, 32, P.smem_bytes, st>>>(P, ch, phase, (u32)n, arrays, bind_mask, barrier_state, epoch,
+                                            burnin_completed, partially_sorted, init_ranks, adjust,
+                                            prng_state, outs, (const ulonglong2*)jump_table, gscratch);
   return cuda_fail(cudaGetLastError(), "phase_kernel launch", errbuf, errlen);
 }
 

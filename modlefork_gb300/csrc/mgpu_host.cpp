@@ -553,6 +553,10 @@ struct mgpu_ctx {
   std::vector<ChromEntry> chroms;
   std::mutex mu;
   u64 smem_limit = 0;
+  u64 smem_budget = 0;     // per-cell shared memory the layout planner may use (0 = limit)
+  uint32_t debug_flags = 0;
+  char* d_scratch = nullptr;  // per-cell global slots for arrays that do not fit on chip
+  u64 scratch_bytes = 0;
 };
 
 extern "C" const char* mgpu_last_error_string(void) { return g_last_error.c_str(); }
@@ -610,6 +614,7 @@ extern "C" int mgpu_destroy(mgpu_ctx* ctx) {
   for (auto& c : ctx->chroms) cudaFree(c.d_bars);
   cudaFree(ctx->d_jump);
   cudaFree(ctx->d_work);
+  cudaFree(ctx->d_scratch);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -746,12 +751,56 @@ static int make_kparams(const mgpu_ctx* ctx, const ChromEntry& ch, uint64_t nlef
   if (UINT64_MAX % (range + 1) == range) ++bucket;
   P->pos_bucket = bucket;
   P->pos_range = range;
-  const u64 smem = cell_smem_bytes(nlefs, ch.nb, P->hist_cap);
-  if (smem > ctx->smem_limit)
-    return fail(MGPU_ERR_UNSUPPORTED,
-                "a cell with %llu LEFs and %u barriers needs %llu B of shared memory (limit %llu)",
-                (unsigned long long)nlefs, ch.nb, (unsigned long long)smem,
-                (unsigned long long)ctx->smem_limit);
+  P->debug_flags = ctx->debug_flags;
+  // Layout: the header (scalars, PRNG ring, burn-in history, barrier bits) is always on chip;
+  // per-LEF arrays go on chip in priority order while they fit, the rest into a global slot.
+  const u64 header = cell_header_bytes(ch.nb, P->hist_cap);
+  const u64 limit = std::min<u64>(ctx->smem_limit, ctx->smem_budget ? ctx->smem_budget : ctx->smem_limit);
+  if (header > limit)
+    return fail(MGPU_ERR_UNSUPPORTED, "%u barriers need %llu B of shared memory (limit %llu)", ch.nb,
+                (unsigned long long)header, (unsigned long long)limit);
+  const u64 arr_bytes = ((u64)nlefs * 4 + 15) & ~15ull;
+  u64 smem_used = header, slot_used = 0;
+  P->arr_smem = 0;
+  const int groups[][2] = {{ARR_REV, -1}, {ARR_FWD, -1}, {ARR_RR, -1}, {ARR_FR, -1}, {ARR_RM, -1},
+                           {ARR_FM, -1},  {ARR_RC, -1},  {ARR_FC, -1}, {ARR_SR, ARR_SF}, {ARR_TMP, -1},
+                           {ARR_BEP, -1}};
+  for (const auto& g : groups) {
+    const u64 bytes = g[1] < 0 ? arr_bytes : (((u64)nlefs * 8 + 15) & ~15ull);
+    const bool on_chip = smem_used + bytes <= limit;
+    u64& used = on_chip ? smem_used : slot_used;
+    P->arr_off[g[0]] = (u32)used;
+    if (g[1] >= 0) P->arr_off[g[1]] = (u32)(used + (u64)nlefs * 4);  // SF right after SR
+    if (on_chip) {
+      P->arr_smem |= 1u << g[0];
+      if (g[1] >= 0) P->arr_smem |= 1u << g[1];
+    }
+    used += bytes;
+  }
+  P->smem_bytes = (u32)smem_used;
+  P->slot_bytes = slot_used;
+  return MGPU_OK;
+}
+
+// Make sure the context's global scratch holds `cells` slots of the plan's size.
+static int ensure_scratch(mgpu_ctx* ctx, const KParams& P, u64 cells) {
+  const u64 need = P.slot_bytes * cells;
+  if (need <= ctx->scratch_bytes) return MGPU_OK;
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->user_stream) cudaStreamSynchronize(ctx->user_stream);
+  cudaFree(ctx->d_scratch);
+  ctx->d_scratch = nullptr;
+  ctx->scratch_bytes = 0;
+  CK(cudaMalloc(&ctx->d_scratch, need));
+  ctx->scratch_bytes = need;
+  return MGPU_OK;
+}
+
+extern "C" int mgpu_set_debug_flags(mgpu_ctx* ctx, uint32_t flags, uint64_t smem_budget) {
+  if (!ctx) return fail(MGPU_ERR_INVALID_ARG, "mgpu_set_debug_flags: null context");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->debug_flags = flags;
+  ctx->smem_budget = smem_budget;
   return MGPU_OK;
 }
 
@@ -844,10 +893,14 @@ static int run_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* seeds, const u
   d_stats.owned = true;
   char err[256] = {0};
   DevChrom dc{ch.d_bars, ch.nb};
+  if (P.slot_bytes) {
+    rc = ensure_scratch(ctx, P, resident_cells(P, ncells));
+    if (rc) return rc;
+  }
   CK(cudaEventRecord(ctx->ev0, st));
   rc = launch_simulate(P, dc, (const CellTask*)d_tasks.p, ncells, target_epochs, (u32*)d_band.p,
                        (u64*)d_missed.p, (mgpu_cell_stats*)d_stats.p, trace, ctx->d_jump,
-                       ctx->d_work, st, err, sizeof(err));
+                       ctx->d_work, ctx->d_scratch, ctx->scratch_bytes, st, err, sizeof(err));
   if (rc) return fail(rc, "%s", err);
   CK(cudaEventRecord(ctx->ev1, st));
   if (band && d_band.owned) CK(cudaMemcpyAsync(band, d_band.p, band_bytes, cudaMemcpyDeviceToHost, st));
@@ -1020,10 +1073,14 @@ extern "C" int mgpu_run_phase(mgpu_ctx* ctx, int chrom_id, int phase, mgpu_phase
   CK(cudaMemset(d_outs.p, 0, 32));
   char err[256] = {0};
   DevChrom dc{ch.d_bars, ch.nb};
+  if (P.slot_bytes) {
+    rc = ensure_scratch(ctx, P, 1);
+    if (rc) return rc;
+  }
   rc = launch_phase(P, dc, phase, n, (uint64_t*)d_arr.p, (uint64_t*)d_mask.p, (uint8_t*)d_bst.p,
                     io->epoch, io->burnin_completed, io->ranks_partially_sorted, io->init_ranks,
                     io->adjust_moves, (uint64_t*)d_prng.p, (uint64_t*)d_outs.p, ctx->d_jump,
-                    active_stream(ctx), err, sizeof(err));
+                    ctx->d_scratch, active_stream(ctx), err, sizeof(err));
   if (rc) return fail(rc, "%s", err);
   CK(cudaStreamSynchronize(active_stream(ctx)));
   for (int k = 0; k < 9; ++k)

@@ -100,6 +100,28 @@ struct KParams {
   // binding positions: uniform_int[start, end - 1]
   u64 pos_bucket;
   u64 pos_range;
+  // per-LEF array layout (planned on the host): byte offset of each array inside the shared
+  // memory of the cell or inside its global scratch slot
+  u32 arr_off[12];
+  u32 arr_smem;    // bit k set: array k lives in shared memory
+  u32 smem_bytes;  // dynamic shared memory of one cell
+  u64 slot_bytes;  // global scratch of one resident cell (arrays that do not fit on chip)
+  u32 debug_flags; // DBG_* bits: force the exact serial implementation of a step
+};
+
+// Per-LEF arrays of a cell, in on-chip placement priority order.  SR and SF are adjacent:
+// together they also serve as a double-precision scratch of nlefs entries.
+enum : u32 {
+  ARR_REV = 0, ARR_FWD, ARR_RR, ARR_FR, ARR_RM, ARR_FM, ARR_RC, ARR_FC, ARR_SR, ARR_SF,
+  ARR_TMP, ARR_BEP, NARR
+};
+constexpr u32 CELL_HEADER_BYTES = 256;  // per-cell scalars at the start of shared memory
+
+enum : u32 {
+  DBG_SERIAL_RANK = 1u << 0,
+  DBG_SERIAL_ADJUST = 1u << 1,
+  DBG_SERIAL_COLLISIONS = 1u << 2,
+  DBG_SERIAL_CONTACTS = 1u << 3,
 };
 
 struct CellTask {
@@ -127,14 +149,12 @@ enum : u32 {
   DEV_ERR_NO_BOUND_LEF = 4,  // contact sampling found no bound LEF within bounds
 };
 
-// Shared-memory footprint of one cell.
-MGPU_HD inline u64 cell_smem_bytes(u64 nlefs, u64 nbarriers, u64 hist_cap) {
-  const u64 scalars = 512;
+// Fixed part of a cell's shared memory: scalars, PRNG ring, burn-in history, barrier bits.
+MGPU_HD inline u64 cell_header_bytes(u64 nbarriers, u64 hist_cap) {
   const u64 ring = (u64)RING * 8;
   const u64 hist = 2 * hist_cap * 8;
-  const u64 bars = ((nbarriers + 31) / 32) * 4;
-  const u64 lefs = 10 * nlefs * 4;
-  return scalars + ring + hist + ((bars + 15) & ~15ull) + lefs;
+  const u64 bars = (((nbarriers + 31) / 32) * 4 + 15) & ~15ull;
+  return CELL_HEADER_BYTES + ring + hist + bars;
 }
 
 // Host side helpers implemented in mgpu_host.cpp, device launchers in mgpu_device.cu.
@@ -146,11 +166,13 @@ struct DevChrom {
 int launch_simulate(const KParams& P, const DevChrom& ch, const CellTask* tasks, u64 ncells,
                     u64 target_epochs, u32* band, u64* missed, mgpu_cell_stats* stats,
                     const DevTrace* trace, const void* jump_table, u32* work_counter,
-                    void* stream, char* errbuf, int errlen);
+                    char* gscratch, u64 gscratch_bytes, void* stream, char* errbuf, int errlen);
+// Number of cells resident at once for a launch (grid size of the persistent kernel).
+u64 resident_cells(const KParams& P, u64 ncells);
 int launch_phase(const KParams& P, const DevChrom& ch, int phase, u64 n, u64* arrays,
                  u64* bind_mask, uint8_t* barrier_state, u64 epoch, u32 burnin_completed,
                  u32 partially_sorted, u32 init_ranks, u32 adjust, u64* prng_state, u64* outs,
-                 const void* jump_table, void* stream, char* errbuf, int errlen);
+                 const void* jump_table, char* gscratch, void* stream, char* errbuf, int errlen);
 u64 max_smem_per_block();
 
 }  // namespace mgpu

@@ -64,6 +64,7 @@ def load(path=LIB_PATH):
         "mgpu_prng_seed": (None, [u64, P(u64)]),
         "mgpu_set_stream": (i32, [C.c_void_p, C.c_void_p]),
         "mgpu_last_kernel_ms": (i32, [C.c_void_p, P(C.c_double)]),
+        "mgpu_set_debug_flags": (i32, [C.c_void_p, C.c_uint32, u64]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(lib, name)
@@ -254,6 +255,11 @@ class Engine:
         ms = C.c_double()
         _check(self.lib.mgpu_last_kernel_ms(self.h, C.byref(ms)), "mgpu_last_kernel_ms")
         return ms.value
+
+    def set_debug_flags(self, flags=0, smem_budget=0):
+        """Force the serial restatement of some steps (bit 0 rank, 1 adjust, 2 collisions,
+        3 contacts) and/or cap a cell's shared memory (bytes, 0 = device limit)."""
+        _check(self.lib.mgpu_set_debug_flags(self.h, flags, smem_budget), "mgpu_set_debug_flags")
 
     def run_phase(self, chrom_id, phase, io):
         return self.lib.mgpu_run_phase(self.h, chrom_id, phase, C.byref(io))

@@ -25,11 +25,18 @@ pytestmark = pytest.mark.gpu
 CASES = load_golden_cases()
 
 
+# execution modes of the engine: warp-parallel steps, the serial restatements forced, and the
+# per-LEF arrays moved to global scratch (the layout of very large cells)
+MODES = {"fast": (0, 0), "serial": (0xF, 0), "global_scratch": (0, 12 * 1024)}
+
+
+@pytest.mark.parametrize("mode", list(MODES))
 @pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
-def test_gpu_matches_reference_unit_test(case):
+def test_gpu_matches_reference_unit_test(case, mode):
     overrides, chrom, barriers, _ = golden_inputs(case)
     cfg = engine.config_defaults(**overrides)
     with engine.Engine(cfg) as eng:
+        eng.set_debug_flags(*MODES[mode])
         cid = eng.upload_chrom(engine.Chromosome("chr1", chrom["size"], chrom["start"], chrom["end"]),
                                barriers)
         st = run_golden_case(case, lambda phase, io: eng.run_phase(cid, phase, io))
@@ -73,7 +80,7 @@ def first_divergence(g_arrays, o_arrays, nl, nrec):
     return "no difference in the recorded arrays"
 
 
-def compare_cell(cfg, chrom, bars, cell_id=0, nl=None, max_epochs=20000, target=None):
+def compare_cell(cfg, chrom, bars, cell_id=0, nl=None, max_epochs=20000, target=None, mode="fast"):
     nl = nl or engine.num_lefs(cfg, chrom.simulated_size)
     targets, te = engine.task_targets(cfg, chrom.simulated_size, nl, int(cfg.num_cells))
     target = int(targets[min(cell_id, len(targets) - 1)]) if target is None else target
@@ -81,6 +88,7 @@ def compare_cell(cfg, chrom, bars, cell_id=0, nl=None, max_epochs=20000, target=
     nrows, ncols = engine.band_shape(cfg, chrom.simulated_size)
     gband = np.zeros(nrows * ncols, dtype=np.uint32)
     with engine.Engine(cfg) as eng:
+        eng.set_debug_flags(*MODES[mode])
         cid = eng.upload_chrom(chrom, bars)
         gst, _, _, ghdr, gn = eng.trace_cell(cid, seed, target, te, nl, max_epochs=max_epochs, band=gband)
         rc, ost, ohdr, on, oband, _ = oracle_trace(cfg, chrom, bars, seed, target, te, nl, max_epochs)
@@ -117,11 +125,12 @@ def small_genome(cfg, length, nbarriers, seed, occupancy=None, name="chrT", star
     return chrom, bars
 
 
+@pytest.mark.parametrize("mode", list(MODES))
 @pytest.mark.parametrize("cell", [0, 1, 17, 63])
-def test_parity_10mbp_cell(cell):
+def test_parity_10mbp_cell(cell, mode):
     cfg, gen = genome.parity_10mbp(seed=7)
     chrom, bars = gen[0]
-    st = compare_cell(cfg, chrom, bars, cell_id=cell)
+    st = compare_cell(cfg, chrom, bars, cell_id=cell, mode=mode)
     assert st.burnin_epochs > 100 and st.contacts > 0
 
 
@@ -145,8 +154,9 @@ STRESS = {
 }
 
 
+@pytest.mark.parametrize("mode", list(MODES))
 @pytest.mark.parametrize("name", list(STRESS))
-def test_stress_cell(name):
+def test_stress_cell(name, mode):
     ov, length, nb, occ = STRESS[name]
     ov = dict(ov)
     burn_target = ov.pop("burnin_target_epochs_for_lef_activation", None)
@@ -156,7 +166,7 @@ def test_stress_cell(name):
     start = 1_234_567 if name == "offset_start" else 0
     chrom, bars = small_genome(cfg, length, nb, seed=sum(map(ord, name)), occupancy=occ, start=start)
     for cell in (0, 5):
-        compare_cell(cfg, chrom, bars, cell_id=cell, max_epochs=50000)
+        compare_cell(cfg, chrom, bars, cell_id=cell, max_epochs=50000, mode=mode)
 
 
 def test_batch_matches_oracle_cells():
