@@ -231,6 +231,14 @@ int mgpu_last_kernel_ms(mgpu_ctx* ctx, double* ms);
  * remaining per-LEF arrays in global scratch. */
 int mgpu_set_debug_flags(mgpu_ctx* ctx, uint32_t flags, uint64_t smem_budget);
 
+/* Profile of the last mgpu_simulate_cells launch (no counterpart in the reference): SM cycles
+ * spent in each step of the epoch summed over cells (entries 0-15: burn-in, bind, rank,
+ * contacts, moves, adjust, barriers, boundaries, LEF-BAR, primary, corrections, secondary,
+ * fix, extrude+release, trace, total) and event counts (16: rank fallbacks, 17: adjust
+ * fallbacks, 18: serial chain walks, 19: serial contact attempts, 20: fix fallbacks,
+ * 21: PRNG refills, 22: refills after serial draws, 23: epochs). */
+int mgpu_last_profile(mgpu_ctx* ctx, uint64_t counters[32]);
+
 /* Upload one chromosome and its barriers (sorted with mgpu_sort_barriers order); returns a
  * handle in *chrom_id.  Barriers are shared by every cell of the chromosome. */
 int mgpu_upload_chrom(mgpu_ctx* ctx, const mgpu_chrom* chrom, const mgpu_barrier* barriers,

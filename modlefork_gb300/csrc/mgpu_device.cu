@@ -83,6 +83,14 @@ __device__ __forceinline__ u32 warp_excl_scan(u32 v, u32* total) {
 }
 
 // Cell scalars (warp-uniform, kept in shared memory so lane 0's serial code can update them).
+// Per-launch profile counters (cycles per step and fallback counts), summed over cells.
+enum : u32 {
+  PF_BURNIN = 0, PF_BIND, PF_RANK, PF_CONTACTS, PF_MOVES, PF_ADJUST, PF_BARRIERS, PF_BOUNDARIES,
+  PF_LEF_BAR, PF_PRIMARY, PF_CORRECT, PF_SECONDARY, PF_FIX, PF_EXTRUDE_RELEASE, PF_TRACE, PF_TOTAL,
+  PF_RANK_FALLBACK, PF_ADJUST_FALLBACK, PF_CHAIN_SERIAL, PF_CONTACT_SERIAL, PF_FIX_FALLBACK,
+  PF_REFILLS, PF_STALE_REFILLS, PF_EPOCHS, PF_RANK_PDQ, PF_COUNT = 32
+};
+
 struct Scalars {
   u64 rpos, gpos;  // next draw to consume / to generate (stream indices)
   u64 canon[4];    // xoshiro state at gpos
@@ -94,6 +102,7 @@ struct Scalars {
   u64 n5, n3;
   u32 hist_size, hist_head;
   u64 bc0, bc1, bc2;  // broadcast slots for lane 0 results
+  u64* prof;          // profile counters of the launch (device memory) or null
 };
 static_assert(sizeof(Scalars) <= CELL_HEADER_BYTES, "scalars do not fit the cell header");
 
@@ -136,9 +145,14 @@ __device__ __forceinline__ void xo_jump(u64* s, const ulonglong2* jt) {
 __device__ __noinline__ void rng_refill(Cell& c, u64* s) {
   Scalars* sc = c.sc;
   const u32 lane = ln();
-  if (sc->lanes_stale) {
+  const bool stale = sc->lanes_stale != 0;
+  if (stale) {
     for (int k = 0; k < 4; ++k) s[k] = sc->canon[k];
     for (u32 t = 0; t < lane * RNG_S; ++t) xo_next(s);
+  }
+  if (lane == 0 && sc->prof) {
+    atomicAdd((unsigned long long*)&sc->prof[PF_REFILLS], 1ull);
+    if (stale) atomicAdd((unsigned long long*)&sc->prof[PF_STALE_REFILLS], 1ull);
   }
   const u64 g = sc->gpos;
 #pragma unroll 4
@@ -172,6 +186,10 @@ __device__ u64 rng_serial(Cell& c) {
   const u64 v = c.ring[sc->rpos & (RING - 1)];
   sc->rpos++;
   return v;
+}
+
+__device__ __forceinline__ void prof_add(Cell& c, u32 k, u64 v) {
+  if (ln() == 0 && c.sc->prof) atomicAdd((unsigned long long*)&c.sc->prof[k], (unsigned long long)v);
 }
 
 __device__ __forceinline__ void set_status(Cell& c, u32 st) {
@@ -910,81 +928,232 @@ __device__ __forceinline__ u64 rank_key(const Cell& c, u32 dir, u32 idx) {
   return ((u64)p << 32) | e;
 }
 
-// rank_lefs for one direction, warp-parallel.  The units bound this epoch (set M) are the
-// only ones whose positions jumped; the others (set S) keep the previous rank order.  If S
-// is still strictly increasing in (position, epoch key) and all keys are distinct, the
-// reference's result is the unique sorted order, built here as a merge of S with sorted M.
-// Returns false (nothing written) when that does not hold: the caller then runs the exact
-// split_sort / pdq_sort emulation.
-__device__ bool rank_dir_fast(Cell& c, u32 dir, u32 n, u32 epoch) {
+// Warp bitonic sort of a[0..m) by ranking key.  Only ascending comparators are used (each merge
+// starts by comparing mirror pairs), so the virtual +inf padding up to a power of two never
+// moves and needs no storage.
+__device__ void bitonic_by_key(const Cell& c, u32 dir, u32* a, u32 m) {
+  u32 p2 = 1;
+  while (p2 < m) p2 <<= 1;
+  auto cmpx = [&](u32 i, u32 j) {
+    if (j >= m) return;
+    const u32 x = a[i], y = a[j];
+    if (rank_key(c, dir, x) > rank_key(c, dir, y)) {
+      a[i] = y;
+      a[j] = x;
+    }
+  };
+  for (u32 size = 2; size <= p2; size <<= 1) {
+    const u32 half = size >> 1;
+    for (u32 t = ln(); t < p2 / 2; t += 32) {
+      const u32 base = (t / half) * size, off = t % half;
+      cmpx(base + off, base + size - 1 - off);
+    }
+    __syncwarp();
+    for (u32 stride = half >> 1; stride > 0; stride >>= 1) {
+      for (u32 t = ln(); t < p2 / 2; t += 32) {
+        const u32 i = 2 * stride * (t / stride) + (t % stride);
+        cmpx(i, i + stride);
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// Lane 0: insertion-sort the run of equal positions around a[t-1], a[t] by binding epoch
+// (ascending for rev units, descending for fwd units), as the tie fix of rank_lefs does
+// (simulation.cpp:446-485).  Returns the end of the run.
+__device__ u32 tie_fix_run(const Cell& c, u32 dir, u32* a, u32 t, u32 len) {
+  const u32* pos = dir ? c.fwd : c.rev;
+  const u32 p = pos[a[t]];
+  u32 lo = t - 1, hi = t + 1;
+  while (lo > 0 && pos[a[lo - 1]] == p) --lo;
+  while (hi < len && pos[a[hi]] == p) ++hi;
+  if (dir) {
+    ins_sort(a, lo, hi, KeyCmpRev{c.bep});
+  } else {
+    ins_sort(a, lo, hi, KeyCmp{c.bep});
+  }
+  return hi;
+}
+
+// rank_lefs for one direction when the previous order is reused (split_sort,
+// simulation.cpp:427-435, then the tie fix :446-485), warp-parallel and exact.
+//
+// split_sort makes one pass that keeps a non-decreasing stack K of the input (a smaller
+// element pops the stack top and both leave), pdq-sorts the removed elements B in the order the
+// pass's swaps leave them, and merges K and B stably.  The tie fix then orders runs of equal
+// positions by binding epoch.  The result is the stable sort of K followed by B by the key
+// (position, epoch): the order is unique except among full ties (equal position and epoch),
+// which keep K's order, then B's order after pdq_sort.
+//
+// Here the pass runs 32 elements at a time: the lanes up to the first one below its
+// predecessor (or below the stack top) are pushed together, and each pop is an event.  The
+// removed block only changes by events (top prepended, reader appended) and by pushes (each
+// rotates it left by one), so every removed element's final slot follows from the event list.
+// B is sorted by key with a warp bitonic sort; only if B holds full ties is it pdq-sorted
+// exactly on lane 0.  Returns false (R untouched) when the event list does not fit.
+__device__ bool rank_dir_split(Cell& c, u32 dir, u32 n) {
+  if (n < 2 || n > 0xFFFFu) return false;
   u32* R = dir ? c.fr : c.rr;
-  u32* Sidx = c.sr;
-  u32* Midx = c.tmp;
-  u32* Msort = c.sf;
-  u32 ns = 0, nm = 0;
-  for (u32 base = 0; base < n; base += 32) {
-    const u32 i = base + ln();
-    const bool valid = i < n;
-    const u32 idx = valid ? R[i] : 0;
-    const bool isM = valid && c.bep[idx] == epoch;
-    const bool isS = valid && !isM;
-    const unsigned ms = __ballot_sync(FULL, isS), mm = __ballot_sync(FULL, isM);
-    if (isS) Sidx[ns + __popc(ms & lanemask_lt())] = idx;
-    if (isM) Midx[nm + __popc(mm & lanemask_lt())] = idx;
-    ns += __popc(ms);
-    nm += __popc(mm);
-  }
-  __syncwarp();
-  if (nm > 1024) return false;
-  bool bad = false;
-  for (u32 k = ln() + 1; k < ns; k += 32) {
-    if (!(rank_key(c, dir, Sidx[k - 1]) < rank_key(c, dir, Sidx[k]))) bad = true;
-  }
-  if (__any_sync(FULL, bad)) return false;
-  // sort M by counting ranks; distinct keys required
-  for (u32 a = ln(); a < nm; a += 32) {
-    const u64 ka = rank_key(c, dir, Midx[a]);
-    u32 r = 0;
-    for (u32 b = 0; b < nm; ++b) {
-      const u64 kb = rank_key(c, dir, Midx[b]);
-      r += kb < ka;
-      bad |= (kb == ka) && (b != a);
+  const u32* pos = dir ? c.fwd : c.rev;
+  u32* K = c.sr;
+  const u32 EMAX = n / 3;
+  u32* ev_q = c.sf;  // pushes since the previous event; later (q mod k_prev) | k_prev << 16
+  u32* ev_top = c.sf + EMAX;
+  u32* ev_rd = c.sf + 2 * EMAX;
+  u32* B = c.tmp;
+  const u32 lane = ln();
+  const u32 first = R[0];
+  if (lane == 0) K[0] = first;
+  u32 m = 0, T = pos[first], E = 0, q = 0;
+  for (u32 base = 1; base < n; base += 32) {
+    const u32 r = base + lane;
+    const u32 nvalid = min(32u, n - base);
+    const bool valid = lane < nvalid;
+    const u32 idx = valid ? R[r] : 0;
+    const u32 v = valid ? pos[idx] : 0;
+    const u32 vprev = __shfl_up_sync(FULL, v, 1);
+    const bool pre_ok = lane == 0 || v >= vprev;
+    u32 start = 0;
+    while (start < nvalid) {
+      const bool ok = lane == start ? v >= T : pre_ok;
+      const unsigned fail = __ballot_sync(FULL, !ok && lane >= start && valid);
+      const u32 f = fail ? (u32)(__ffs(fail) - 1) : nvalid;
+      if (lane >= start && lane < f) K[m + 1 + lane - start] = idx;
+      if (f > start) {
+        m += f - start;
+        if (E) q += f - start;
+        T = __shfl_sync(FULL, v, f - 1);
+      }
+      if (f == nvalid) break;
+      const u32 rd = __shfl_sync(FULL, idx, f);
+      if (E >= EMAX) return false;
+      __syncwarp();
+      u32 top = UNBOUND;
+      if (m > 0) {
+        top = K[m];
+        --m;
+        T = pos[K[m]];
+      }
+      if (lane == 0) {
+        ev_q[E] = q;
+        ev_top[E] = top;
+        ev_rd[E] = rd;
+      }
+      ++E;
+      q = 0;
+      start = f + 1;
     }
-    if (!bad) Msort[r] = Midx[a];
   }
-  if (__any_sync(FULL, bad)) return false;
   __syncwarp();
-  // no M key may equal an S key
-  for (u32 m = ln(); m < nm; m += 32) {
-    const u64 km = rank_key(c, dir, Msort[m]);
+  const u32 ns = m + 1;
+  // block size before each event, and the rotation it saw since the previous event
+  u32 kacc = 0;
+  for (u32 b = 0; b < E; b += 32) {
+    const u32 j = b + lane;
+    const bool vj = j < E;
+    const u32 sz = vj ? (ev_top[j] != UNBOUND ? 2u : 1u) : 0u;
+    u32 tot;
+    const u32 ex = warp_excl_scan(sz, &tot);
+    if (vj) {
+      const u32 kprev = kacc + ex;
+      const u32 qm = kprev ? ev_q[j] % kprev : 0u;
+      ev_q[j] = qm | (kprev << 16);
+    }
+    kacc += tot;
+  }
+  const u32 kE = kacc;
+  __syncwarp();
+  // final slot of every removed element
+  const u32 qfm = kE ? q % kE : 0u;
+  for (u32 b = 0; b < E; b += 32) {
+    const u32 j = b + lane;
+    const bool vj = j < E;
+    const u32 top = vj ? ev_top[j] : UNBOUND;
+    const u32 rd = vj ? ev_rd[j] : 0u;
+    const u32 kj = vj ? (ev_q[j] >> 16) + (top != UNBOUND ? 2u : 1u) : 1u;
+    u32 it = 0, ir = kj - 1;
+    for (u32 jj = b + 1; jj < E; ++jj) {
+      const u32 w = ev_q[jj];
+      const bool pop = ev_top[jj] != UNBOUND;
+      if (jj > j) {
+        const u32 qm = w & 0xFFFFu, kk = w >> 16;
+        it = it >= qm ? it - qm : it + kk - qm;
+        ir = ir >= qm ? ir - qm : ir + kk - qm;
+        if (pop) {
+          ++it;
+          ++ir;
+        }
+      }
+    }
+    it = it >= qfm ? it - qfm : it + kE - qfm;
+    ir = ir >= qfm ? ir - qfm : ir + kE - qfm;
+    if (vj) {
+      if (top != UNBOUND) B[it] = top;
+      B[ir] = rd;
+    }
+  }
+  __syncwarp();
+  // sort B by key (events are dead: sf is free)
+  u32* Bs = c.sf;
+  for (u32 t = lane; t < kE; t += 32) Bs[t] = B[t];
+  __syncwarp();
+  bitonic_by_key(c, dir, Bs, kE);
+  bool full_tie = false;
+  for (u32 t = lane + 1; t < kE; t += 32) full_tie |= rank_key(c, dir, Bs[t - 1]) == rank_key(c, dir, Bs[t]);
+  const u32* Bf = Bs;
+  if (__any_sync(FULL, full_tie)) {
+    prof_add(c, PF_RANK_PDQ, 1);
+    if (lane == 0) {
+      pdq_sort(B, 0, kE, KeyCmp{pos});
+      for (u32 t = 1; t < kE; ++t) {
+        if (pos[B[t - 1]] == pos[B[t]]) t = tie_fix_run(c, dir, B, t, kE);
+      }
+    }
+    __syncwarp();
+    Bf = B;
+  }
+  // tie fix of K: runs of equal positions whose epochs are out of order
+  for (u32 base = 1; base < ns; base += 32) {
+    const u32 t = base + lane;
+    bool bad = false;
+    if (t < ns) {
+      const u32 a0 = K[t - 1], a1 = K[t];
+      bad = pos[a0] == pos[a1] && rank_key(c, dir, a0) > rank_key(c, dir, a1);
+    }
+    unsigned bm = __ballot_sync(FULL, bad);
+    if (bm) {
+      if (lane == 0) {
+        while (bm) {
+          const u32 t0 = base + (u32)(__ffs(bm) - 1);
+          const u32 hi = tie_fix_run(c, dir, K, t0, ns);
+          const u32 last = hi - 1 - base;  // bits up to the run's end are done
+          bm = last >= 31 ? 0u : bm & ~((2u << last) - 1u);
+        }
+      }
+      __syncwarp();
+    }
+  }
+  // merge: K first among equal keys
+  for (u32 i = lane; i < ns; i += 32) {
+    const u32 idx = K[i];
+    const u64 key = rank_key(c, dir, idx);
+    u32 lo = 0, hi = kE;
+    while (lo < hi) {
+      const u32 mid = (lo + hi) >> 1;
+      if (rank_key(c, dir, Bf[mid]) < key) lo = mid + 1; else hi = mid;
+    }
+    R[i + lo] = idx;
+  }
+  for (u32 j = lane; j < kE; j += 32) {
+    const u32 idx = Bf[j];
+    const u64 key = rank_key(c, dir, idx);
     u32 lo = 0, hi = ns;
     while (lo < hi) {
       const u32 mid = (lo + hi) >> 1;
-      if (rank_key(c, dir, Sidx[mid]) < km) lo = mid + 1; else hi = mid;
+      if (rank_key(c, dir, K[mid]) <= key) lo = mid + 1; else hi = mid;
     }
-    if (lo < ns && rank_key(c, dir, Sidx[lo]) == km) bad = true;
-  }
-  if (__any_sync(FULL, bad)) return false;
-  // merge
-  for (u32 sidx = ln(); sidx < ns; sidx += 32) {
-    const u32 idx = Sidx[sidx];
-    const u64 ks = rank_key(c, dir, idx);
-    u32 lo = 0, hi = nm;
-    while (lo < hi) {
-      const u32 mid = (lo + hi) >> 1;
-      if (rank_key(c, dir, Msort[mid]) < ks) lo = mid + 1; else hi = mid;
-    }
-    R[sidx + lo] = idx;
-  }
-  for (u32 m = ln(); m < nm; m += 32) {
-    const u32 idx = Msort[m];
-    const u64 km = rank_key(c, dir, idx);
-    u32 lo = 0, hi = ns;
-    while (lo < hi) {
-      const u32 mid = (lo + hi) >> 1;
-      if (rank_key(c, dir, Sidx[mid]) < km) lo = mid + 1; else hi = mid;
-    }
-    R[m + lo] = idx;
+    R[j + lo] = idx;
   }
   __syncwarp();
   return true;
@@ -992,8 +1161,9 @@ __device__ bool rank_dir_fast(Cell& c, u32 dir, u32 n, u32 epoch) {
 
 __device__ void rank_lefs(Cell& c, const KParams& P, u32 n, u32 epoch, bool partially_sorted) {
   for (u32 dir = 0; dir < 2; ++dir) {
-    const bool ok = !(P.debug_flags & DBG_SERIAL_RANK) && rank_dir_fast(c, dir, n, epoch);
+    const bool ok = partially_sorted && !(P.debug_flags & DBG_SERIAL_RANK) && rank_dir_split(c, dir, n);
     if (!ok) {
+      prof_add(c, PF_RANK_FALLBACK, 1);
       if (ln() == 0) {
         rank_dir_serial(c, dir, n, partially_sorted);
         c.sc->sort_fallbacks++;
@@ -1156,10 +1326,12 @@ __device__ bool adjust_fwd_fast(Cell& c, const KParams& P, u32 n) {
 __device__ void adjust_moves(Cell& c, const KParams& P, u32 n) {
   const bool serial = P.debug_flags & DBG_SERIAL_ADJUST;
   if (serial || !adjust_rev_fast(c, P, n)) {
+    prof_add(c, PF_ADJUST_FALLBACK, 1);
     if (ln() == 0) adjust_dir_serial(c, P, 0, n);
     __syncwarp();
   }
   if (serial || !adjust_fwd_fast(c, P, n)) {
+    prof_add(c, PF_ADJUST_FALLBACK, 1);
     if (ln() == 0) adjust_dir_serial(c, P, 1, n);
     __syncwarp();
   }
@@ -1478,6 +1650,7 @@ __device__ void secondary_dir_fast(Cell& c, u64* s, const KParams& P, u32 dir, u
     const unsigned over = __ballot_sync(FULL, ci < nst && off + Ld > RNG_BLOCK);
     const u32 fb = over ? (u32)(__ffs(over) - 1) : 32u;
     if (fb == 0) {  // a single chain longer than the ring window: walk it serially
+      prof_add(c, PF_CHAIN_SERIAL, 1);
       if (ln() == 0) {
         u32 used;
         chain_walk<CHAIN_SERIAL>(c, P, dir, n, starts[q], 0, &used);
@@ -1545,6 +1718,7 @@ __device__ bool fix_secondary_fast(Cell& c, const KParams& P, u32 n, u64 n5, u64
 // process_collisions (simulation.cpp:925-955) in the reference's order.
 __device__ void process_collisions(Cell& c, u64* s, const KParams& P, u32 n, bool fix) {
   Scalars* sc = c.sc;
+  u64 t0 = clock64();
   const bool serial = (P.debug_flags & DBG_SERIAL_COLLISIONS) || !ranked_sorted(c, n);
   __syncwarp();
   if (ln() == 0) {
@@ -1554,6 +1728,8 @@ __device__ void process_collisions(Cell& c, u64* s, const KParams& P, u32 n, boo
     sc->n3 = n3;
   }
   __syncwarp();
+  u64 t1 = clock64();
+  prof_add(c, PF_BOUNDARIES, t1 - t0);
   const u64 n5 = sc->n5, n3 = sc->n3;
   if (serial) {
     rng_ensure(c, s, RNG_BLOCK);
@@ -1564,10 +1740,17 @@ __device__ void process_collisions(Cell& c, u64* s, const KParams& P, u32 n, boo
     __syncwarp();
   } else {
     detect_lef_bar_fast(c, s, P, n, n5, n3);
+    t0 = clock64();
+    prof_add(c, PF_LEF_BAR, t0 - t1);
+    t1 = t0;
     detect_primary_fast(c, s, P, n, n5, n3);
   }
+  t0 = clock64();
+  prof_add(c, PF_PRIMARY, t0 - t1);
   correct_lef_bar(c, n);
   correct_primary(c, n);
+  t1 = clock64();
+  prof_add(c, PF_CORRECT, t1 - t0);
   if (serial) {
     rng_ensure(c, s, RNG_BLOCK);
     if (ln() == 0) process_secondary_serial(c, P, n, n5, n3);
@@ -1577,12 +1760,16 @@ __device__ void process_collisions(Cell& c, u64* s, const KParams& P, u32 n, boo
     secondary_dir_fast(c, s, P, 0, n, n5, n3);
     secondary_dir_fast(c, s, P, 1, n, n5, n3);
   }
+  t0 = clock64();
+  prof_add(c, PF_SECONDARY, t0 - t1);
   if (fix) {
     if (serial || !fix_secondary_fast(c, P, n, n5, n3)) {
+      prof_add(c, PF_FIX_FALLBACK, 1);
       if (ln() == 0) fix_secondary_serial(c, P, n, n5, n3);
       __syncwarp();
     }
   }
+  prof_add(c, PF_FIX, clock64() - t0);
 }
 
 // extrude (simulation.cpp:489-512)
@@ -1898,6 +2085,7 @@ __device__ void sample_contacts(Cell& c, u64* s, const KParams& P, u64 target) {
       __syncwarp();
       if (todo != 0 && lim == f && f < 32) {
         // attempt f could not be evaluated from the ring: run it serially
+        prof_add(c, PF_CONTACT_SERIAL, 1);
         if (ln() == 0) {
           bool sok, smiss;
           contact_attempt_serial(c, P, tad, na, &sok, &smiss);
@@ -2085,6 +2273,8 @@ __device__ void run_cell(Cell& c, u64* s, const KParams& P, const CellTask& task
   Scalars* sc = c.sc;
   const u32 nl = P.nlefs;
   cell_reset(c, nl, task.seed);
+  if (ln() == 0) sc->prof = P.prof;
+  __syncwarp();
   barriers_init(c, s);
   if (P.skip_burnin && ln() == 0) {
     sc->num_active = nl;
@@ -2096,13 +2286,20 @@ __device__ void run_cell(Cell& c, u64* s, const KParams& P, const CellTask& task
     const bool go = P.contact_mode ? (sc->num_contacts < target)
                                    : (sc->epoch - sc->num_burnin_epochs < target_epochs);
     if (!go) break;
+    const u64 te0 = clock64();
     if (!sc->burnin_completed) run_burnin(c, s, P);
+    u64 ta = clock64();
+    prof_add(c, PF_BURNIN, ta - te0);
     const u32 n = (u32)sc->num_active;
     const u32 epoch = (u32)sc->epoch;
     const bool completed = sc->burnin_completed != 0;
     if (ln() == 0) sc->lef_epochs += n;
     bind_lefs(c, s, P, n, epoch, 0, nullptr);
+    u64 tb = clock64();
+    prof_add(c, PF_BIND, tb - ta);
     rank_lefs(c, P, n, epoch, epoch != 0);
+    ta = clock64();
+    prof_add(c, PF_RANK, ta - tb);
     if (completed) {
       if (P.debug_flags & DBG_SERIAL_CONTACTS) {
         rng_ensure(c, s, RNG_BLOCK);
@@ -2111,26 +2308,44 @@ __device__ void run_cell(Cell& c, u64* s, const KParams& P, const CellTask& task
       } else {
         sample_contacts(c, s, P, target);
       }
-      if (target != 0 && sc->num_contacts >= target) break;
+      tb = clock64();
+      prof_add(c, PF_CONTACTS, tb - ta);
+      ta = tb;
+      if (target != 0 && sc->num_contacts >= target) {
+        prof_add(c, PF_TOTAL, clock64() - te0);
+        break;
+      }
       if (sc->status != DEV_OK) break;
     }
     gen_moves_dir(c, s, c.rm, n, P.rev_speed[completed], P.rev_std, P.rev_move_int[completed]);
     gen_moves_dir(c, s, c.fm, n, P.fwd_speed[completed], P.fwd_std, P.fwd_move_int[completed]);
+    tb = clock64();
+    prof_add(c, PF_MOVES, tb - ta);
     gather_ranked(c, n);
     adjust_moves(c, P, n);
     clamp_moves(c, P, n);
+    ta = clock64();
+    prof_add(c, PF_ADJUST, ta - tb);
     barriers_next(c, s);
     for (u32 i = ln(); i < n; i += 32) {
       c.rc[i] = 0;
       c.fc[i] = 0;
     }
     __syncwarp();
+    tb = clock64();
+    prof_add(c, PF_BARRIERS, tb - ta);
     process_collisions(c, s, P, n, true);
+    ta = clock64();
     extrude(c, n);
     release_lefs(c, s, P, n, completed);
+    tb = clock64();
+    prof_add(c, PF_EXTRUDE_RELEASE, tb - ta);
     if (trace) trace_record(c, P, *trace, sc->epoch);
     if (ln() == 0) sc->epoch++;
     __syncwarp();
+    prof_add(c, PF_TRACE, clock64() - tb);
+    prof_add(c, PF_TOTAL, clock64() - te0);
+    prof_add(c, PF_EPOCHS, 1);
     if (sc->status != DEV_OK) break;
   }
   if (ln() == 0) {
@@ -2214,6 +2429,7 @@ __global__ void __launch_bounds__(32) phase_kernel(const __grid_constant__ KPara
     sc->num_active = n;
     sc->burnin_completed = burnin_completed;
     sc->sort_fallbacks = 0;
+    sc->prof = nullptr;
   }
   __syncwarp();
   const bool completed = burnin_completed != 0;

@@ -557,6 +557,8 @@ struct mgpu_ctx {
   uint32_t debug_flags = 0;
   char* d_scratch = nullptr;  // per-cell global slots for arrays that do not fit on chip
   u64 scratch_bytes = 0;
+  uint64_t* d_prof = nullptr;  // profile counters of the last launch
+  uint64_t h_prof[32] = {0};
 };
 
 extern "C" const char* mgpu_last_error_string(void) { return g_last_error.c_str(); }
@@ -596,6 +598,7 @@ extern "C" int mgpu_create(int device, const mgpu_config* cfg, mgpu_ctx** out) {
   if (!rc) rc = cuda_check(cudaMalloc(&ctx->d_jump, jt.size() * 8), "cudaMalloc(jump table)");
   if (!rc) rc = cuda_check(cudaMemcpy(ctx->d_jump, jt.data(), jt.size() * 8, cudaMemcpyHostToDevice), "copy jump table");
   if (!rc) rc = cuda_check(cudaMalloc(&ctx->d_work, sizeof(u32)), "cudaMalloc(work counter)");
+  if (!rc) rc = cuda_check(cudaMalloc(&ctx->d_prof, 32 * sizeof(uint64_t)), "cudaMalloc(profile)");
   if (!rc) rc = cuda_check(cudaEventCreate(&ctx->ev0), "cudaEventCreate");
   if (!rc) rc = cuda_check(cudaEventCreate(&ctx->ev1), "cudaEventCreate");
   if (rc) {
@@ -615,6 +618,7 @@ extern "C" int mgpu_destroy(mgpu_ctx* ctx) {
   cudaFree(ctx->d_jump);
   cudaFree(ctx->d_work);
   cudaFree(ctx->d_scratch);
+  cudaFree(ctx->d_prof);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -796,6 +800,12 @@ static int ensure_scratch(mgpu_ctx* ctx, const KParams& P, u64 cells) {
   return MGPU_OK;
 }
 
+extern "C" int mgpu_last_profile(mgpu_ctx* ctx, uint64_t counters[32]) {
+  if (!ctx || !counters) return fail(MGPU_ERR_INVALID_ARG, "mgpu_last_profile: null argument");
+  std::memcpy(counters, ctx->h_prof, sizeof(ctx->h_prof));
+  return MGPU_OK;
+}
+
 extern "C" int mgpu_set_debug_flags(mgpu_ctx* ctx, uint32_t flags, uint64_t smem_budget) {
   if (!ctx) return fail(MGPU_ERR_INVALID_ARG, "mgpu_set_debug_flags: null context");
   std::lock_guard<std::mutex> lk(ctx->mu);
@@ -897,6 +907,8 @@ static int run_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* seeds, const u
     rc = ensure_scratch(ctx, P, resident_cells(P, ncells));
     if (rc) return rc;
   }
+  P.prof = ctx->d_prof;
+  CK(cudaMemsetAsync(ctx->d_prof, 0, 32 * sizeof(uint64_t), st));
   CK(cudaEventRecord(ctx->ev0, st));
   rc = launch_simulate(P, dc, (const CellTask*)d_tasks.p, ncells, target_epochs, (u32*)d_band.p,
                        (u64*)d_missed.p, (mgpu_cell_stats*)d_stats.p, trace, ctx->d_jump,
@@ -908,6 +920,7 @@ static int run_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* seeds, const u
   CK(cudaMemcpyAsync(&h_missed, d_missed.p, 8, cudaMemcpyDeviceToHost, st));
   std::vector<mgpu_cell_stats> h_stats(ncells);
   CK(cudaMemcpyAsync(h_stats.data(), d_stats.p, ncells * sizeof(mgpu_cell_stats), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(ctx->h_prof, ctx->d_prof, 32 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   {
     float ms = 0.f;

@@ -107,6 +107,7 @@ struct KParams {
   u32 smem_bytes;  // dynamic shared memory of one cell
   u64 slot_bytes;  // global scratch of one resident cell (arrays that do not fit on chip)
   u32 debug_flags; // DBG_* bits: force the exact serial implementation of a step
+  u64* prof;       // per-launch profile counters (32 entries, device memory) or null
 };
 
 // Per-LEF arrays of a cell, in on-chip placement priority order.  SR and SF are adjacent:

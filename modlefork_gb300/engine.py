@@ -65,6 +65,7 @@ def load(path=LIB_PATH):
         "mgpu_set_stream": (i32, [C.c_void_p, C.c_void_p]),
         "mgpu_last_kernel_ms": (i32, [C.c_void_p, P(C.c_double)]),
         "mgpu_set_debug_flags": (i32, [C.c_void_p, C.c_uint32, u64]),
+        "mgpu_last_profile": (i32, [C.c_void_p, P(u64)]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(lib, name)
@@ -260,6 +261,17 @@ class Engine:
         """Force the serial restatement of some steps (bit 0 rank, 1 adjust, 2 collisions,
         3 contacts) and/or cap a cell's shared memory (bytes, 0 = device limit)."""
         _check(self.lib.mgpu_set_debug_flags(self.h, flags, smem_budget), "mgpu_set_debug_flags")
+
+    PROFILE_NAMES = ("burnin", "bind", "rank", "contacts", "moves", "adjust", "barriers",
+                     "boundaries", "lef_bar", "primary", "correct", "secondary", "fix",
+                     "extrude_release", "trace", "total", "rank_fallbacks", "adjust_fallbacks",
+                     "serial_chain_walks", "serial_contact_attempts", "fix_fallbacks", "refills",
+                     "stale_refills", "epochs", "rank_pdq")
+
+    def last_profile(self):
+        buf = (C.c_uint64 * 32)()
+        _check(self.lib.mgpu_last_profile(self.h, buf), "mgpu_last_profile")
+        return {name: buf[i] for i, name in enumerate(self.PROFILE_NAMES)}
 
     def run_phase(self, chrom_id, phase, io):
         return self.lib.mgpu_run_phase(self.h, chrom_id, phase, C.byref(io))
