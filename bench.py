@@ -1,11 +1,12 @@
 #!/usr/bin/env python3
 """Benchmark of the loop-extrusion epoch engine on the genome-scale workload.
 
-Workload (one step): 24 synthetic chromosomes, lengths uniform in [50, 250] Mbp, 5 kb bins,
-3 Mbp band, one barrier per 50 kb (Beta(8, 2) occupancy), 20 LEFs/Mbp, 200 kb lifetime,
-512 cells per chromosome, contact density 1, one engine launch per chromosome.  The
-metric is LEF-epochs/s (sum over cells and epochs of active LEFs, burn-in included), with
-cells/s and contacts/s reported beside it.
+Workload: 24 synthetic chromosomes, lengths uniform in [50, 250] Mbp, 5 kb bins, 3 Mbp band,
+one barrier per 50 kb (Beta(8, 2) occupancy), 20 LEFs/Mbp, 200 kb lifetime, 512 cells per
+chromosome, contact density 1, one engine launch per chromosome.  One step is one such launch;
+step i simulates chromosome i mod 24, so 24 steps cover the genome once.  The metric is
+LEF-epochs/s (sum over cells and epochs of active LEFs, burn-in included), with cells/s and
+contacts/s reported beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -39,13 +40,13 @@ WORKLOAD = "genome_24chr_50-250Mbp_5kb_512cells"
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=12)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cells", type=int, default=512, help="cells per chromosome")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline time budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=2)
     return ap.parse_args()
 
 
@@ -209,8 +210,8 @@ def run_reference(args):
     for _ in range(args.warmup):
         cpu_sample(cfg, tasks[0], 0.1, threads)  # one batch
     rates, samples, secs = [], [], 0.0
-    for _ in range(args.steps):
-        s = cpu_sample(cfg, tasks[0], per_step, threads)
+    for i in range(args.steps):
+        s = cpu_sample(cfg, tasks[i % len(tasks)], per_step, threads)
         rates.append(s["lef_epochs"] / s["seconds"])
         samples.append(s)
         secs += s["seconds"]
@@ -230,6 +231,10 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def log(msg):
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
 def run_ours(args):
     import torch
 
@@ -244,6 +249,7 @@ def run_ours(args):
 
     mbuild.build()
     cfg, tasks = build_workload(args.cells, rank)
+    log("workload ready")
     eng = engine.Engine(cfg, local)
     stream = torch.cuda.current_stream()
     eng.set_stream(stream.cuda_stream)
@@ -254,22 +260,23 @@ def run_ours(args):
         t["d_targets"] = torch.from_numpy(t["targets"].view(np.int64)).to(dev)
         t["d_band"] = torch.zeros(t["nrows"] * t["ncols"], dtype=torch.int32, device=dev)
 
-    def step(record):
+    def step(i, record):
+        t = tasks[i % len(tasks)]
+        log(f"step {i} ({'timed' if record else 'warm-up'}): {t['chrom'].name}, {t['nlefs']} LEFs")
+        _, st = eng.simulate_cells(t["cid"], t["d_seeds"].data_ptr(), t["d_targets"].data_ptr(),
+                                   t["te"], t["nlefs"], t["d_band"].data_ptr(), ncells=len(t["seeds"]))
         tot = dict(lef_epochs=0, cells=0, contacts=0, bytes=0, kernel_ms=0.0, launches=0)
-        for t in tasks:
-            _, st = eng.simulate_cells(t["cid"], t["d_seeds"].data_ptr(), t["d_targets"].data_ptr(),
-                                       t["te"], t["nlefs"], t["d_band"].data_ptr())
-            if record:
-                tot["lef_epochs"] += sum(s.lef_epochs for s in st)
-                tot["contacts"] += sum(s.contacts for s in st)
-                tot["cells"] += len(st)
-                tot["bytes"] += algorithmic_bytes(st, len(t["bars"]))
-                tot["kernel_ms"] += eng.last_kernel_ms()
-                tot["launches"] += 1
+        if record:
+            tot["lef_epochs"] = sum(s.lef_epochs for s in st)
+            tot["contacts"] = sum(s.contacts for s in st)
+            tot["cells"] = len(st)
+            tot["bytes"] = algorithmic_bytes(st, len(t["bars"]))
+            tot["kernel_ms"] = eng.last_kernel_ms()
+            tot["launches"] = 1
         return tot
 
-    for _ in range(args.warmup):
-        step(False)
+    for i in range(args.warmup):
+        step(i, False)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -278,8 +285,8 @@ def run_ours(args):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     agg = dict(lef_epochs=0, cells=0, contacts=0, bytes=0, kernel_ms=0.0, launches=0)
-    for _ in range(args.steps):
-        s = step(True)
+    for i in range(args.steps):
+        s = step(i, True)
         for k in agg:
             agg[k] += s[k]
     ev1.record(stream)
@@ -298,24 +305,25 @@ def run_ours(args):
             agg[k] = v.item()
         dist.barrier()
 
+    log(f"timed region: {ms:.1f} ms")
     # end to end through the C ABI with host buffers
     e2e = None
     if args.e2e_steps > 0:
-        host_bands = [np.zeros(t["nrows"] * t["ncols"], dtype=np.uint32) for t in tasks]
+        host_bands = [np.zeros(t["nrows"] * t["ncols"], dtype=np.uint32) for t in tasks[:args.e2e_steps]]
         eng.set_stream(None)
         torch.cuda.synchronize()
         h2d = d2h = 0
         le = 0
         t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            for t, hb in zip(tasks, host_bands):
-                _, st = eng.simulate_cells(t["cid"], t["seeds"], t["targets"], t["te"], t["nlefs"], hb)
-                le += sum(s.lef_epochs for s in st)
-                h2d += t["seeds"].nbytes + t["targets"].nbytes + hb.nbytes
-                d2h += hb.nbytes + len(st) * C.sizeof(st[0])
+        for i in range(args.e2e_steps):
+            t, hb = tasks[i % len(tasks)], host_bands[i % len(tasks)]
+            _, st = eng.simulate_cells(t["cid"], t["seeds"], t["targets"], t["te"], t["nlefs"], hb)
+            le += sum(s.lef_epochs for s in st)
+            h2d += t["seeds"].nbytes + t["targets"].nbytes + hb.nbytes
+            d2h += hb.nbytes + len(st) * C.sizeof(st[0])
         dt = time.perf_counter() - t0
         e2e = {"value": le / dt, "unit": "LEF-epochs/s", "h2d_bytes_per_step": h2d // args.e2e_steps,
-               "d2h_bytes_per_step": d2h // args.e2e_steps}
+               "d2h_bytes_per_step": d2h // args.e2e_steps, "steps": args.e2e_steps}
 
     if rank != 0:
         return
@@ -328,6 +336,9 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32+f64",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "chromosomes": len(tasks), "cells_per_chromosome": args.cells,
+                   "step": "one launch: 512 cells of chromosome (i mod 24)",
+                   "timed_chromosomes": sorted({tasks[i % len(tasks)]["chrom"].name for i in range(args.steps)},
+                                               key=lambda x: int(x[3:])),
                    "genome_bp": int(sum(t["chrom"].size for t in tasks)),
                    "lefs": int(sum(t["nlefs"] for t in tasks)),
                    "barriers": int(sum(len(t["bars"]) for t in tasks)),
@@ -342,6 +353,7 @@ def run_ours(args):
         "e2e": e2e, "clocks": clk,
     }
     if not args.no_cpu_baseline:
+        log("cpu baseline")
         threads = os.cpu_count() or 1
         s = cpu_sample(cfg, tasks[0], args.cpu_seconds, threads)
         line["cpu_baseline"] = {"value": s["lef_epochs"] / s["seconds"], "unit": "LEF-epochs/s",

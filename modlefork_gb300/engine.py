@@ -206,12 +206,29 @@ class Engine:
         return cid.value
 
     def simulate_cells(self, chrom_id, seeds, targets, target_epochs, nlefs, band=None,
-                       stats=True):
-        """Simulate len(seeds) cells; contacts are added into ``band`` (numpy uint32 array or
-        device pointer).  Returns (missed_updates, per-cell stats array or None)."""
-        seeds = np.ascontiguousarray(seeds, dtype=np.uint64)
-        targets = np.ascontiguousarray(targets, dtype=np.uint64)
-        n = len(seeds)
+                       stats=True, ncells=None):
+        """Simulate the cells given by ``seeds`` and ``targets``; contacts are added into
+        ``band``.  Each of seeds, targets and band is either a host numpy array or a device
+        pointer (an int, e.g. a torch tensor's data_ptr()); with device seeds and targets
+        ``ncells`` is required.  Returns (missed_updates, per-cell stats array or None)."""
+        def as_ptr(a, dtype, name):
+            if isinstance(a, (int, np.integer)):
+                if ncells is None:
+                    raise ValueError(f"{name} is a device pointer: pass ncells")
+                return int(a), None
+            arr = np.ascontiguousarray(a, dtype=dtype)
+            if arr.ndim != 1:
+                raise ValueError(f"{name} must be one-dimensional")
+            return arr.ctypes.data, arr
+
+        seeds_ptr, seeds_arr = as_ptr(seeds, np.uint64, "seeds")
+        targets_ptr, targets_arr = as_ptr(targets, np.uint64, "targets")
+        sizes = {len(a) for a in (seeds_arr, targets_arr) if a is not None}
+        if ncells is not None:
+            sizes.add(int(ncells))
+        if len(sizes) != 1:
+            raise ValueError(f"seeds, targets and ncells disagree on the number of cells: {sizes}")
+        n = sizes.pop()
         missed = C.c_uint64(0)
         st = (abi.CellStats * n)() if stats else None
         if isinstance(band, np.ndarray):
@@ -219,7 +236,7 @@ class Engine:
             band_ptr = band.ctypes.data
         else:
             band_ptr = band
-        _check(self.lib.mgpu_simulate_cells(self.h, chrom_id, seeds.ctypes.data, targets.ctypes.data,
+        _check(self.lib.mgpu_simulate_cells(self.h, chrom_id, seeds_ptr, targets_ptr,
                                             target_epochs, nlefs, n, band_ptr,
                                             C.addressof(missed), C.addressof(st) if st else None),
                "mgpu_simulate_cells")

@@ -57,3 +57,38 @@ def simulate_genome(cfg, genome, ncells=None, device=0, simulate_wo_barriers=Fal
                                                t["nlefs"], band)
             out.append(ChromResult(chrom, t["nlefs"], band, missed, stats))
     return out
+
+
+def _main(argv=None):
+    """Run one workload and print its throughput, e.g. for profiling one launch:
+
+    python -m modlefork_gb300.simulate --workload genome --chrom 0 --cells 64
+    """
+    import argparse
+    import json
+    import time
+
+    from . import genome as gen
+
+    ap = argparse.ArgumentParser(description=_main.__doc__)
+    ap.add_argument("--workload", choices=["parity", "genome"], default="genome")
+    ap.add_argument("--chrom", type=int, action="append", help="chromosome index (repeatable)")
+    ap.add_argument("--cells", type=int, default=None)
+    ap.add_argument("--device", type=int, default=0)
+    args = ap.parse_args(argv)
+    cfg, g = gen.parity_10mbp() if args.workload == "parity" else gen.genome_24chr()
+    if args.chrom:
+        g = [g[i] for i in args.chrom]
+    if args.cells is not None:
+        cfg.num_cells = args.cells
+    t0 = time.perf_counter()
+    res = simulate_genome(cfg, g, device=args.device)
+    dt = time.perf_counter() - t0
+    le = sum(r.lef_epochs for r in res)
+    print(json.dumps({"workload": args.workload, "chromosomes": [r.chrom.name for r in res],
+                      "cells": int(cfg.num_cells), "lef_epochs": le, "contacts": sum(r.contacts for r in res),
+                      "wall_s": dt, "lef_epochs_per_s": le / dt}))
+
+
+if __name__ == "__main__":
+    _main()

@@ -218,6 +218,37 @@ def test_host_buffers_accumulate_into_band():
     assert np.array_equal(band, 2 * once)
 
 
+def test_device_buffers_match_host_buffers():
+    """Seeds, targets and band given as device pointers (torch tensors) give the same band
+    and statistics as host arrays, on a caller's stream."""
+    torch = pytest.importorskip("torch")
+    cfg, gen = genome.parity_10mbp(seed=9)
+    chrom, bars = gen[0]
+    nl = engine.num_lefs(cfg, chrom.simulated_size)
+    n = 8
+    targets, te = engine.task_targets(cfg, chrom.simulated_size, nl, n)
+    seeds = np.arange(n, dtype=np.uint64) + 1234
+    nrows, ncols = engine.band_shape(cfg, chrom.simulated_size)
+    hband = np.zeros(nrows * ncols, dtype=np.uint32)
+    dev = torch.device("cuda", 0)
+    d_seeds = torch.from_numpy(seeds.view(np.int64)).to(dev)
+    d_targets = torch.from_numpy(targets.view(np.int64)).to(dev)
+    d_band = torch.zeros(nrows * ncols, dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream()
+    with engine.Engine(cfg) as eng:
+        cid = eng.upload_chrom(chrom, bars)
+        hm, hst = eng.simulate_cells(cid, seeds, targets, te, nl, hband)
+        with pytest.raises(ValueError):
+            eng.simulate_cells(cid, d_seeds.data_ptr(), d_targets.data_ptr(), te, nl, d_band.data_ptr())
+        eng.set_stream(stream.cuda_stream)
+        dm, dst = eng.simulate_cells(cid, d_seeds.data_ptr(), d_targets.data_ptr(), te, nl,
+                                     d_band.data_ptr(), ncells=n)
+    torch.cuda.synchronize()
+    assert dm == hm
+    assert [(s.epochs, s.contacts, s.rng_draws) for s in dst] == [(s.epochs, s.contacts, s.rng_draws) for s in hst]
+    assert np.array_equal(d_band.cpu().numpy().view(np.uint32), hband)
+
+
 def test_unreachable_contacts_end_with_timeout_status():
     """A chromosome where no LEF can ever be inside (start + 1, end - 1) would make the
     reference loop forever; the device gives up after its attempt budget and reports it."""
