@@ -264,6 +264,40 @@ int mgpu_simulate_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* cell_seeds,
                         uint64_t num_lefs, uint64_t ncells, uint32_t* band,
                         uint64_t* missed_updates, mgpu_cell_stats* stats);
 
+/*
+ * mgpu_simulate_cells without any memory allocation (no counterpart in the reference, whose
+ * worker threads allocate their State buffers once and reuse them).
+ *
+ * For callers that must not allocate device memory while they run: a process whose GPU memory
+ * is all held by another allocator (a framework's caching pool, say), a loop with a fixed
+ * memory budget, or a loop that cannot afford the device-wide synchronisation a cudaFree
+ * implies.  The call needs a little scratch space (the per-cell task list, the work counter
+ * and, for chromosomes whose per-LEF arrays do not fit in one block's shared memory, one
+ * global slot per concurrently simulated cell); it takes it from one fixed array of
+ * MGPU_NOALLOC_SCRATCH_BYTES that is part of the loaded library, one per device.
+ *
+ *   - Every buffer must be device memory: cell_seeds, target_contacts and band are required,
+ *     missed_updates (added to, like mgpu_simulate_cells) and stats may be NULL.
+ *   - ncells may be at most MGPU_NOALLOC_MAX_CELLS; larger batches, host pointers and
+ *     chromosomes whose global slot does not fit the scratch are rejected with
+ *     MGPU_ERR_INVALID_ARG / MGPU_ERR_UNSUPPORTED and a message, before any work is issued.
+ *   - The work counter in the scratch is cleared on the stream before each launch.
+ *   - The call only enqueues work on the context's stream and returns; the results are ready
+ *     after mgpu_sync (or when the stream completes).  Errors detected on the device (the
+ *     per-cell status) are reported through stats[i].status, not through the return value.
+ *   - The first call on a device looks up the scratch's address (cudaGetSymbolAddress) with
+ *     that device current; make that first call before capturing the stream.
+ *   - The scratch is shared by every context of the process on that device, so calls that
+ *     overlap in time (two streams, two contexts, two threads) race on it and give wrong
+ *     results: issue them on one stream, or synchronise between them.
+ */
+#define MGPU_NOALLOC_SCRATCH_BYTES (8u << 20)
+#define MGPU_NOALLOC_MAX_CELLS 16384u
+int mgpu_simulate_cells_noalloc(mgpu_ctx* ctx, int chrom_id, const uint64_t* cell_seeds,
+                                const uint64_t* target_contacts, uint64_t target_epochs,
+                                uint64_t num_lefs, uint64_t ncells, uint32_t* band,
+                                uint64_t* missed_updates, mgpu_cell_stats* stats);
+
 /* ---- parity and debugging entry points (used by the test-suite) ------------------------ */
 
 /*

@@ -15,6 +15,8 @@ MGPU_ERR_UNSUPPORTED = -5
 MGPU_ERR_NO_DEVICE = -6
 MGPU_ERR_OUT_OF_MEMORY = -7
 MGPU_ERR_INTERNAL = -8
+MGPU_NOALLOC_SCRATCH_BYTES = 8 << 20
+MGPU_NOALLOC_MAX_CELLS = 16384
 
 STATUS_NAMES = {
     0: "MGPU_OK", -1: "MGPU_ERR_INVALID_ARG", -2: "MGPU_ERR_CUDA", -3: "MGPU_ERR_TIMEOUT",

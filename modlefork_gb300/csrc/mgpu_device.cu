@@ -2639,4 +2639,28 @@ int launch_phase(const KParams& P, const DevChrom& ch, int phase, u64 n, u64* ar
   return cuda_fail(cudaGetLastError(), "phase_kernel launch", errbuf, errlen);
 }
 
+// ---------------------------------------------------------------------------------------
+// Fixed scratch of the allocation-free entry point (one array per device, part of the module)
+// ---------------------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MGPU_NOALLOC_SCRATCH_BYTES];
+
+__global__ void pack_tasks_kernel(const u64* seeds, const u64* targets, u64 n, CellTask* tasks) {
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
+    tasks[i].seed = seeds[i];
+    tasks[i].target_contacts = targets[i];
+  }
+}
+
+int noalloc_scratch_address(void** ptr, char* errbuf, int errlen) {
+  return cuda_fail(cudaGetSymbolAddress(ptr, g_noalloc_scratch), "cudaGetSymbolAddress", errbuf, errlen);
+}
+
+int launch_pack_tasks(const u64* seeds, const u64* targets, u64 n, CellTask* tasks, void* stream,
+                      char* errbuf, int errlen) {
+  if (n == 0) return MGPU_OK;
+  const u64 blocks = (n + 255) / 256;
+  pack_tasks_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(seeds, targets, n, tasks);
+  return cuda_fail(cudaGetLastError(), "pack_tasks_kernel launch", errbuf, errlen);
+}
+
 }  // namespace mgpu

@@ -958,6 +958,75 @@ extern "C" int mgpu_simulate_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* 
                    band, missed_updates, stats, nullptr);
 }
 
+// Address of the fixed scratch, looked up once per device (with that device current).
+static std::mutex g_noalloc_mu;
+static constexpr int NOALLOC_MAX_DEVICES = 64;
+static void* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+
+extern "C" int mgpu_simulate_cells_noalloc(mgpu_ctx* ctx, int chrom_id, const uint64_t* cell_seeds,
+                                           const uint64_t* target_contacts, uint64_t target_epochs,
+                                           uint64_t num_lefs, uint64_t ncells, uint32_t* band,
+                                           uint64_t* missed_updates, mgpu_cell_stats* stats) {
+  if (!ctx) return fail(MGPU_ERR_INVALID_ARG, "mgpu_simulate_cells_noalloc: null context");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  CK(cudaSetDevice(ctx->device));
+  if (chrom_id < 0 || chrom_id >= (int)ctx->chroms.size())
+    return fail(MGPU_ERR_INVALID_ARG, "unknown chromosome handle %d", chrom_id);
+  if (ncells > MGPU_NOALLOC_MAX_CELLS)
+    return fail(MGPU_ERR_INVALID_ARG,
+                "mgpu_simulate_cells_noalloc: %llu cells requested, the fixed scratch holds at most %u "
+                "(split the batch or use mgpu_simulate_cells)",
+                (unsigned long long)ncells, MGPU_NOALLOC_MAX_CELLS);
+  if (ncells == 0) return MGPU_OK;
+  const void* need_dev[3] = {cell_seeds, target_contacts, band};
+  const char* names[5] = {"cell_seeds", "target_contacts", "band", "missed_updates", "stats"};
+  for (int k = 0; k < 3; ++k) {
+    if (!is_device_ptr(need_dev[k]))
+      return fail(MGPU_ERR_INVALID_ARG, "mgpu_simulate_cells_noalloc: %s must be a device pointer", names[k]);
+  }
+  if (missed_updates && !is_device_ptr(missed_updates))
+    return fail(MGPU_ERR_INVALID_ARG, "mgpu_simulate_cells_noalloc: %s must be a device pointer or NULL", names[3]);
+  if (stats && !is_device_ptr(stats))
+    return fail(MGPU_ERR_INVALID_ARG, "mgpu_simulate_cells_noalloc: %s must be a device pointer or NULL", names[4]);
+  const ChromEntry& ch = ctx->chroms[chrom_id];
+  KParams P;
+  int rc = make_kparams(ctx, ch, num_lefs, &P);
+  if (rc) return rc;
+  if (ctx->device < 0 || ctx->device >= NOALLOC_MAX_DEVICES)
+    return fail(MGPU_ERR_UNSUPPORTED, "mgpu_simulate_cells_noalloc: device %d out of range", ctx->device);
+  char err[256] = {0};
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_addr[ctx->device]) {
+      rc = noalloc_scratch_address(&g_noalloc_addr[ctx->device], err, sizeof(err));
+      if (rc) {
+        g_noalloc_addr[ctx->device] = nullptr;
+        return fail(rc, "%s", err);
+      }
+    }
+    base = g_noalloc_addr[ctx->device];
+  }
+  char* scratch = (char*)base;
+  const u64 slot_room = MGPU_NOALLOC_SCRATCH_BYTES - NOALLOC_SLOTS_OFFSET;
+  if (P.slot_bytes > slot_room)
+    return fail(MGPU_ERR_UNSUPPORTED,
+                "mgpu_simulate_cells_noalloc: %llu LEFs need %llu B of global scratch per cell, the fixed "
+                "scratch has %llu B for cell slots",
+                (unsigned long long)num_lefs, (unsigned long long)P.slot_bytes, (unsigned long long)slot_room);
+  P.prof = nullptr;
+  cudaStream_t st = active_stream(ctx);
+  CellTask* tasks = (CellTask*)(scratch + NOALLOC_TASKS_OFFSET);
+  rc = launch_pack_tasks(cell_seeds, target_contacts, ncells, tasks, st, err, sizeof(err));
+  if (rc) return fail(rc, "%s", err);
+  DevChrom dc{ch.d_bars, ch.nb};
+  rc = launch_simulate(P, dc, tasks, ncells, target_epochs, band, missed_updates, stats, nullptr,
+                       ctx->d_jump, (u32*)scratch, scratch + NOALLOC_SLOTS_OFFSET, slot_room, st, err,
+                       sizeof(err));
+  if (rc) return fail(rc, "%s", err);
+  return MGPU_OK;
+}
+
 extern "C" int mgpu_trace_cell(mgpu_ctx* ctx, int chrom_id, uint64_t cell_seed,
                                uint64_t target_contacts, uint64_t target_epochs, uint64_t num_lefs,
                                uint32_t* band, mgpu_cell_stats* stats, mgpu_trace_request* tr) {

@@ -176,4 +176,16 @@ int launch_phase(const KParams& P, const DevChrom& ch, int phase, u64 n, u64* ar
                  const void* jump_table, char* gscratch, void* stream, char* errbuf, int errlen);
 u64 max_smem_per_block();
 
+// Fixed scratch of mgpu_simulate_cells_noalloc: [0, 256) work counter, then the task list of
+// up to MGPU_NOALLOC_MAX_CELLS cells, then global cell slots in what is left.
+constexpr u64 NOALLOC_TASKS_OFFSET = 256;
+constexpr u64 NOALLOC_SLOTS_OFFSET =
+    (NOALLOC_TASKS_OFFSET + (u64)MGPU_NOALLOC_MAX_CELLS * sizeof(CellTask) + 255) & ~255ull;
+static_assert(NOALLOC_SLOTS_OFFSET < MGPU_NOALLOC_SCRATCH_BYTES, "task list larger than the scratch");
+// Address of the scratch on the current device.
+int noalloc_scratch_address(void** ptr, char* errbuf, int errlen);
+// tasks[i] = {seeds[i], targets[i]} on the stream.
+int launch_pack_tasks(const u64* seeds, const u64* targets, u64 n, CellTask* tasks, void* stream,
+                      char* errbuf, int errlen);
+
 }  // namespace mgpu

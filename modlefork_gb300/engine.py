@@ -57,6 +57,8 @@ def load(path=LIB_PATH):
         "mgpu_upload_chrom": (i32, [C.c_void_p, P(abi.Chrom), P(abi.Barrier), u64, P(i32)]),
         "mgpu_simulate_cells": (i32, [C.c_void_p, i32, C.c_void_p, C.c_void_p, u64, u64, u64,
                                       C.c_void_p, C.c_void_p, C.c_void_p]),
+        "mgpu_simulate_cells_noalloc": (i32, [C.c_void_p, i32, C.c_void_p, C.c_void_p, u64, u64, u64,
+                                              C.c_void_p, C.c_void_p, C.c_void_p]),
         "mgpu_trace_cell": (i32, [C.c_void_p, i32, u64, u64, u64, u64, C.c_void_p,
                                   P(abi.CellStats), P(abi.TraceRequest)]),
         "mgpu_state_digest": (u64, [u64] + [P(u64)] * 9),
@@ -242,6 +244,14 @@ class Engine:
                "mgpu_simulate_cells")
         return missed.value, st
 
+    def simulate_cells_noalloc(self, chrom_id, seeds_ptr, targets_ptr, target_epochs, nlefs, ncells,
+                               band_ptr, missed_ptr=None, stats_ptr=None):
+        """mgpu_simulate_cells_noalloc: every argument buffer is a device pointer (int); the
+        work is only enqueued on the context's stream (call sync() before reading results)."""
+        _check(self.lib.mgpu_simulate_cells_noalloc(self.h, chrom_id, seeds_ptr, targets_ptr, target_epochs,
+                                                    nlefs, ncells, band_ptr, missed_ptr, stats_ptr),
+               "mgpu_simulate_cells_noalloc")
+
     def trace_cell(self, chrom_id, seed, target, target_epochs, nlefs, max_records=0,
                    max_epochs=0, band=None):
         """Run one cell recording per-epoch state; returns (stats, headers, arrays, all_headers)."""
@@ -268,6 +278,10 @@ class Engine:
     def set_stream(self, stream_handle):
         """Launch on a caller's cudaStream_t (an int handle, e.g. torch's stream.cuda_stream)."""
         _check(self.lib.mgpu_set_stream(self.h, C.c_void_p(stream_handle)), "mgpu_set_stream")
+
+    def sync(self):
+        """mgpu_sync: wait for the work issued on the context's stream."""
+        _check(self.lib.mgpu_sync(self.h), "mgpu_sync")
 
     def last_kernel_ms(self):
         ms = C.c_double()
