@@ -215,7 +215,8 @@ int mgpu_abi_version(void);
  * simulation.cpp:58-105).  The config is copied. */
 int mgpu_create(int device, const mgpu_config* cfg, mgpu_ctx** out);
 int mgpu_destroy(mgpu_ctx* ctx);
-/* Wait for every call issued on the context's stream. */
+/* Wait for every call issued on the context's stream (and on the caller's stream set with
+ * mgpu_set_stream). */
 int mgpu_sync(mgpu_ctx* ctx);
 
 /* Instrumentation (no counterpart in the reference): launch on the caller's CUDA stream

@@ -244,63 +244,151 @@ __device__ __forceinline__ double ifp_fraction(u64 u) {
   return (double)(u >> 8) * (1.0 / 72057594037927936.0);
 }
 
-__device__ double s_unit_exponential(Cell& c) {
+// Draw sources of the samplers below.  SerialSrc is lane 0's view of the cell's stream; RingSrc
+// is one lane's view of the pre-generated ring starting at a given stream position, which
+// reports exhaustion instead of generating.
+struct SerialSrc {
+  Cell& c;
+  u32 n;
+  __device__ bool next(u64& u) {
+    u = rng_serial(c);
+    ++n;
+    return true;
+  }
+};
+
+struct RingSrc {
+  const u64* ring;
+  u64 pos, end;
+  u32 n;
+  __device__ bool next(u64& u) {
+    if (pos >= end) return false;
+    u = ring[pos & (RING - 1)];
+    ++pos;
+    ++n;
+    return true;
+  }
+};
+
+// Sampler results: 0 = value produced, 1 = the source ran dry, 2 = iteration limit.
+enum { SMP_OK = 0, SMP_DRY = 1, SMP_LIMIT = 2 };
+
+// y < exp(a) for a <= 0, decided exactly: a float estimate of exp(a) settles it unless y lies
+// within 1e-5 (relative) of the estimate, whose error is below 1e-6; only then is the double
+// exp evaluated.
+__device__ __forceinline__ bool below_exp(double y, double a) {
+  const float ef = expf((float)a);
+  const double d = y - (double)ef;
+  if (fabs(d) > 1e-5 * (double)ef) return d < 0;
+  return y < exp(a);
+}
+
+// uniform_01<double> on one draw per attempt (values equal to 1 are rejected)
+template <class Src>
+__device__ int uniform01_t(Src& g, double& r) {
+  for (int it = 0; it < 1000; ++it) {
+    u64 u;
+    if (!g.next(u)) return SMP_DRY;
+    r = u01_of(u);
+    if (r < 1.0) return SMP_OK;
+  }
+  return SMP_LIMIT;
+}
+
+// unit_exponential_distribution: 256-layer ziggurat with the shift-on-layer-0 tail
+template <class Src>
+__device__ int unit_exponential_t(Src& g, double& out) {
   double shift = 0;
   for (int it = 0; it < 100000; ++it) {
-    const u64 u = rng_serial(c);
+    u64 u;
+    if (!g.next(u)) return SMP_DRY;
     const int i = (int)(u & 0xFF);
     const double x = ifp_fraction(u) * mgpu_zig_exp_x[i];
-    if (x < mgpu_zig_exp_x[i + 1]) return shift + x;
+    if (x < mgpu_zig_exp_x[i + 1]) {
+      out = shift + x;
+      return SMP_OK;
+    }
     if (i == 0) {
       shift += mgpu_zig_exp_x[1];
     } else {
-      const double y01 = s_uniform01(c);
+      double y01;
+      const int r = uniform01_t(g, y01);
+      if (r) return r;
       const double y = mgpu_zig_exp_y[i] + y01 * (mgpu_zig_exp_y[i + 1] - mgpu_zig_exp_y[i]);
-      if (y < exp(-x)) return x + shift;
+      if (below_exp(y, -x)) {
+        out = x + shift;
+        return SMP_OK;
+      }
     }
   }
-  set_status(c, DEV_ERR_ITER_LIMIT);
-  return 0.0;
+  return SMP_LIMIT;
 }
 
-__device__ double s_normal_tail(Cell& c) {
+// tail of the normal ziggurat (Marsaglia's method with two exponentials)
+template <class Src>
+__device__ int normal_tail_t(Src& g, double& out) {
   const double tail_start = mgpu_zig_normal_x[1];
   for (int it = 0; it < 100000; ++it) {
-    const double x = s_unit_exponential(c) / tail_start;
-    const double y = s_unit_exponential(c) / 1.0;
-    if (2 * y > x * x) return x + tail_start;
+    double e1, e2;
+    int r = unit_exponential_t(g, e1);
+    if (r) return r;
+    r = unit_exponential_t(g, e2);
+    if (r) return r;
+    const double x = e1 / tail_start;
+    const double y = e2 / 1.0;
+    if (2 * y > x * x) {
+      out = x + tail_start;
+      return SMP_OK;
+    }
   }
-  set_status(c, DEV_ERR_ITER_LIMIT);
-  return 0.0;
+  return SMP_LIMIT;
 }
 
-// Fast path of unit_normal_distribution for one draw: returns false when the draw falls in a
-// wedge or the tail (the full algorithm is then needed).
-__device__ __forceinline__ bool normal_fast(u64 u, double& z) {
-  const int ii = (int)(u & 0xFF);
-  const double sign = (double)((ii & 1) * 2 - 1);
-  const int i = ii >> 1;
-  const double x = ifp_fraction(u) * mgpu_zig_normal_x[i];
-  z = x * sign;
-  return x < mgpu_zig_normal_x[i + 1];
-}
-
-__device__ double s_unit_normal(Cell& c) {
+// unit_normal_distribution: 128-layer ziggurat, sign from bit 0 of the layer byte
+template <class Src>
+__device__ int unit_normal_t(Src& g, double& out) {
   for (int it = 0; it < 100000; ++it) {
-    const u64 u = rng_serial(c);
+    u64 u;
+    if (!g.next(u)) return SMP_DRY;
     const int ii = (int)(u & 0xFF);
     const int sign = (ii & 1) * 2 - 1;
     const int i = ii >> 1;
     const double x = ifp_fraction(u) * mgpu_zig_normal_x[i];
-    if (x < mgpu_zig_normal_x[i + 1]) return x * sign;
-    if (i == 0) return s_normal_tail(c) * sign;
-    const double y01 = s_uniform01(c);
-    const double y =
-        mgpu_zig_normal_y[i] + y01 * (mgpu_zig_normal_y[i + 1] - mgpu_zig_normal_y[i]);
-    if (y < exp(-(x * x / 2))) return x * sign;
+    if (x < mgpu_zig_normal_x[i + 1]) {
+      out = x * sign;
+      return SMP_OK;
+    }
+    if (i == 0) {
+      double t;
+      const int r = normal_tail_t(g, t);
+      if (r) return r;
+      out = t * sign;
+      return SMP_OK;
+    }
+    double y01;
+    const int r = uniform01_t(g, y01);
+    if (r) return r;
+    const double y = mgpu_zig_normal_y[i] + y01 * (mgpu_zig_normal_y[i + 1] - mgpu_zig_normal_y[i]);
+    if (below_exp(y, -(x * x / 2))) {
+      out = x * sign;
+      return SMP_OK;
+    }
   }
-  set_status(c, DEV_ERR_ITER_LIMIT);
-  return 0.0;
+  return SMP_LIMIT;
+}
+
+__device__ double s_unit_exponential(Cell& c) {
+  SerialSrc g{c, 0};
+  double v = 0.0;
+  if (unit_exponential_t(g, v) != SMP_OK) set_status(c, DEV_ERR_ITER_LIMIT);
+  return v;
+}
+
+__device__ double s_unit_normal(Cell& c) {
+  SerialSrc g{c, 0};
+  double v = 0.0;
+  if (unit_normal_t(g, v) != SMP_OK) set_status(c, DEV_ERR_ITER_LIMIT);
+  return v;
 }
 
 __device__ const double kLogFactorial[10] = {0.0,
@@ -1182,50 +1270,84 @@ __device__ void gather_ranked(Cell& c, u32 n) {
   __syncwarp();
 }
 
-// generate_moves_helper (simulation.cpp:264-290): speculation on the ziggurat fast path; the
-// first item that needs more draws is finished serially by lane 0.
-__device__ __forceinline__ bool normal_fast(u64 u, double& z);
-__device__ double s_unit_normal(Cell& c);
-
+// generate_moves_helper (simulation.cpp:264-290) for one direction: move = round(max(0,
+// normal(mean, sd))) for every bound LEF in index order, unbound ones get 0.
+//
+// The normals are variable-length (a ziggurat wedge takes a second draw, the tail takes
+// exponentials), so the warp evaluates a window of 32 candidate starts at once: lane k runs the
+// whole sampler as if a normal started at stream position rpos + k.  The real starts form the
+// chain s0 = 0, s(j+1) = s(j) + len(s(j)); lane j finds s(j) by binary lifting over the
+// lanes' next-start pointers.  A window serves the normals whose start lies inside it (31 or
+// 32 of them in the common case), in stream order, to the next LEFs in index order.
 __device__ void gen_moves_dir(Cell& c, u64* s, u32* mv, u32 n, double mean, double sd, u64 move_int) {
   if (sd == 0.0) {
     for (u32 i = ln(); i < n; i += 32) mv[i] = c.bep[i] == UNBOUND ? 0u : (u32)move_int;
     __syncwarp();
     return;
   }
-  u32 i0 = 0;
-  while (i0 < n) {
-    rng_ensure(c, s, 64);
-    const u32 i = i0 + ln();
+  // items: the bound LEFs in index order (a compacted list only when some are unbound)
+  u32 nb = 0;
+  for (u32 base = 0; base < n; base += 32) {
+    const u32 i = base + ln();
     const bool need = i < n && c.bep[i] != UNBOUND;
     const unsigned m = __ballot_sync(FULL, need);
-    const u32 off = __popc(m & lanemask_lt());
-    double z = 0;
-    bool ok = true;
-    if (need) ok = normal_fast(ring_at(c, c.sc->rpos + off), z);
-    const unsigned bad = __ballot_sync(FULL, need && !ok);
-    const u32 f = bad ? (u32)(__ffs(bad) - 1) : 32u;
-    if (i < n && ln() < f) {
-      if (need) {
-        const double v = round(fmax(0.0, z * sd + mean));
-        if (v > 4294967295.0) set_status(c, DEV_ERR_MOVE_RANGE);
-        mv[i] = (u32)(u64)v;
-      } else {
-        mv[i] = 0;
-      }
+    if (i < n && !need) mv[i] = 0;
+    if (need) c.tmp[nb + __popc(m & lanemask_lt())] = i;
+    nb += __popc(m);
+  }
+  const bool all = nb == n;
+  __syncwarp();
+  u32 t0 = 0;
+  while (t0 < nb) {
+    rng_ensure(c, s, 96);
+    const u64 r0 = c.sc->rpos;
+    RingSrc g{c.ring, r0 + ln(), c.sc->gpos, 0};
+    double z = 0.0;
+    const int st = unit_normal_t(g, z);
+    const u32 len = g.n;
+    // next-start pointers: 32 = beyond the window, 33 = unknown (the sampler ran dry)
+    u32 J[5];
+    J[0] = st == SMP_OK ? min(ln() + len, 32u) : 33u;
+#pragma unroll
+    for (int b = 1; b < 5; ++b) {
+      const u32 prev = J[b - 1];
+      const u32 v = __shfl_sync(FULL, prev, prev < 32 ? prev : 0);
+      J[b] = prev < 32 ? v : prev;
     }
-    __syncwarp();
-    if (ln() == 0) {
-      c.sc->rpos += __popc(m & (f == 32 ? FULL : ((1u << f) - 1)));
-      if (f < 32) {
+    u32 p = 0;  // start of the ln()-th normal of the window
+#pragma unroll
+    for (int b = 0; b < 5; ++b) {
+      const u32 v = __shfl_sync(FULL, J[b], p < 32 ? p : 0);
+      if (((ln() >> b) & 1) && p < 32) p = v;
+    }
+    // the ln()-th normal is usable when it starts inside the window and its sampler finished
+    const u32 jn = __shfl_sync(FULL, J[0], p < 32 ? p : 0);
+    const u32 m = __popc(__ballot_sync(FULL, p < 32 && jn != 33u));
+    const u32 served = min(m, nb - t0);
+    if (served == 0) {
+      // the first normal needs more draws than the ring holds: take it serially
+      if (ln() == 0) {
         const double zz = s_unit_normal(c);
         const double v = round(fmax(0.0, zz * sd + mean));
         if (v > 4294967295.0) set_status(c, DEV_ERR_MOVE_RANGE);
-        mv[i0 + f] = (u32)(u64)v;
+        mv[all ? t0 : c.tmp[t0]] = (u32)(u64)v;
       }
+      __syncwarp();
+      ++t0;
+      continue;
     }
+    const double zj = __shfl_sync(FULL, z, p < 32 ? p : 0);
+    if (ln() < served) {
+      const double v = round(fmax(0.0, zj * sd + mean));
+      if (v > 4294967295.0) set_status(c, DEV_ERR_MOVE_RANGE);
+      mv[all ? t0 + ln() : c.tmp[t0 + ln()]] = (u32)(u64)v;
+    }
+    const u32 plast = __shfl_sync(FULL, p, served - 1);
+    const u32 llast = __shfl_sync(FULL, len, plast);
     __syncwarp();
-    i0 += (f == 32) ? 32 : f + 1;
+    if (ln() == 0) c.sc->rpos = r0 + plast + llast;
+    __syncwarp();
+    t0 += served;
   }
 }
 
@@ -1840,7 +1962,6 @@ __device__ bool burnin_stats(Cell& c, const KParams& P, u32 n) {
     terms[i] = d * d;
   }
   __syncwarp();
-  bool done = false;
   if (ln() == 0) {
     double ssd = 0.0;
     for (u32 i = 0; i < n; ++i) ssd = ssd + terms[i];
@@ -1853,29 +1974,45 @@ __device__ bool burnin_stats(Cell& c, const KParams& P, u32 n) {
     c.havg[slot] = mean;
     c.hcfx[slot] = sd / mean;
     sc->hist_size++;
-    if (sc->hist_size == cap) {
-      const u32 w = P.smooth_w;
-      auto ratio = [&](const double* d) {
-        u64 nd = 0;
-        for (u32 i1 = 1, i2 = w + 1; i2 != cap; ++i1, ++i2) {
-          double a1 = 0.0, a2 = 0.0;
-          for (u32 k = i1 - 1; k < i2 - 1; ++k) a1 = a1 + d[(sc->hist_head + k) % cap];
-          for (u32 k = i1; k < i2; ++k) a2 = a2 + d[(sc->hist_head + k) % cap];
-          const double n1 = a1 / (double)(i2 - i1), n2 = a2 / (double)(i2 - i1);
-          nd += (n1 > n2) ? 1u : 0u;
-        }
-        return (double)nd / (double)((u64)cap - w - nd);
-      };
-      const double r1 = ratio(c.hcfx);
-      if (r1 >= 0.95 && r1 <= 1.05) {
-        const double r2 = ratio(c.havg);
-        done = r2 >= 0.95 && r2 <= 1.05;
-      }
-    }
-    sc->flag = done ? 1u : 0u;
   }
   __syncwarp();
-  return sc->flag != 0;
+  bool done = false;
+  if (sc->hist_size == cap) {
+    // evaluate_burnin's smoothed-dip ratio: window pairs (i1, i2) = (k + 1, k + 1 + w) for
+    // k < cap - w - 1, one window per lane, each window summed in the reference's order
+    const u32 w = P.smooth_w;
+    const u32 head = sc->hist_head;
+    auto ratio = [&](const double* d) {
+      u32 nd = 0;
+      for (u32 i1 = 1 + ln(); i1 + w < cap; i1 += 32) {
+        const u32 i2 = i1 + w;
+        double a1 = 0.0, a2 = 0.0;
+        u32 k = head + i1 - 1;
+        if (k >= cap) k -= cap;
+        for (u32 t = 0; t < w; ++t) {
+          a1 = a1 + d[k];
+          if (++k == cap) k = 0;
+        }
+        k = head + i1;
+        if (k >= cap) k -= cap;
+        for (u32 t = 0; t < w; ++t) {
+          a2 = a2 + d[k];
+          if (++k == cap) k = 0;
+        }
+        const double n1 = a1 / (double)(i2 - i1), n2 = a2 / (double)(i2 - i1);
+        nd += (n1 > n2) ? 1u : 0u;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) nd += __shfl_xor_sync(FULL, nd, o);
+      return (double)nd / (double)((u64)cap - w - nd);
+    };
+    const double r1 = ratio(c.hcfx);
+    if (r1 >= 0.95 && r1 <= 1.05) {
+      const double r2 = ratio(c.havg);
+      done = r2 >= 0.95 && r2 <= 1.05;
+    }
+  }
+  return done;
 }
 
 // run_burnin (simulation.cpp:1027-1054)
@@ -2576,8 +2713,11 @@ u64 max_smem_per_block() {
 }
 
 u64 resident_cells(const KParams& P, u64 ncells) {
-  if (cudaFuncSetAttribute(simulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem_bytes) !=
-      cudaSuccess) {
+  // The attribute is a per-function permission shared by every thread and context of the
+  // process, so it is always set to the device limit: lowering it for one launch would make a
+  // concurrent launch with a larger plan fail.
+  if (cudaFuncSetAttribute(simulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)max_smem_per_block()) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -2598,7 +2738,7 @@ int launch_simulate(const KParams& P, const DevChrom& ch, const CellTask* tasks,
                     const DevTrace* trace, const void* jump_table, u32* work_counter,
                     char* gscratch, u64 gscratch_bytes, void* stream, char* errbuf, int errlen) {
   int rc = cuda_fail(cudaFuncSetAttribute(simulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)P.smem_bytes),
+                                          (int)max_smem_per_block()),
                      "cudaFuncSetAttribute", errbuf, errlen);
   if (rc) return rc;
   u64 grid = resident_cells(P, ncells);
@@ -2629,7 +2769,7 @@ int launch_phase(const KParams& P, const DevChrom& ch, int phase, u64 n, u64* ar
                  u32 partially_sorted, u32 init_ranks, u32 adjust, u64* prng_state, u64* outs,
                  const void* jump_table, char* gscratch, void* stream, char* errbuf, int errlen) {
   int rc = cuda_fail(cudaFuncSetAttribute(phase_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)P.smem_bytes),
+                                          (int)max_smem_per_block()),
                      "cudaFuncSetAttribute", errbuf, errlen);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;

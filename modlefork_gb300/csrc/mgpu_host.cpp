@@ -630,6 +630,7 @@ extern "C" int mgpu_sync(mgpu_ctx* ctx) {
   if (!ctx) return fail(MGPU_ERR_INVALID_ARG, "mgpu_sync: null context");
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->user_stream) CK(cudaStreamSynchronize(ctx->user_stream));
   return MGPU_OK;
 }
 
@@ -790,12 +791,12 @@ static int make_kparams(const mgpu_ctx* ctx, const ChromEntry& ch, uint64_t nlef
 static int ensure_scratch(mgpu_ctx* ctx, const KParams& P, u64 cells) {
   const u64 need = P.slot_bytes * cells;
   if (need <= ctx->scratch_bytes) return MGPU_OK;
-  cudaStreamSynchronize(ctx->stream);
-  if (ctx->user_stream) cudaStreamSynchronize(ctx->user_stream);
-  cudaFree(ctx->d_scratch);
+  // stream-ordered: the old slots are released after the launches already issued on the stream
+  cudaStream_t st = ctx->user_stream ? ctx->user_stream : ctx->stream;
+  if (ctx->d_scratch) CK(cudaFreeAsync(ctx->d_scratch, st));
   ctx->d_scratch = nullptr;
   ctx->scratch_bytes = 0;
-  CK(cudaMalloc(&ctx->d_scratch, need));
+  CK(cudaMallocAsync((void**)&ctx->d_scratch, need, st));
   ctx->scratch_bytes = need;
   return MGPU_OK;
 }
@@ -824,14 +825,31 @@ static bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-// Device copy of a host or device buffer (RAII).
+// Device buffer (RAII).  Buffers allocated with a stream are stream-ordered
+// (cudaMallocAsync / cudaFreeAsync), so a call never synchronises the whole device and calls
+// of independent contexts overlap.
 struct DevBuf {
   void* p = nullptr;
   bool owned = false;
+  cudaStream_t st = nullptr;
+  bool ordered = false;
   ~DevBuf() {
-    if (owned) cudaFree(p);
+    if (!owned) return;
+    if (ordered) {
+      cudaFreeAsync(p, st);
+    } else {
+      cudaFree(p);
+    }
   }
 };
+
+static int alloc_on_stream(DevBuf& d, size_t bytes, cudaStream_t st) {
+  CK(cudaMallocAsync(&d.p, bytes, st));
+  d.owned = true;
+  d.ordered = true;
+  d.st = st;
+  return MGPU_OK;
+}
 
 static int to_device(const void* src, size_t bytes, DevBuf& d, cudaStream_t st, bool copy) {
   if (!src || bytes == 0) return MGPU_OK;
@@ -839,8 +857,8 @@ static int to_device(const void* src, size_t bytes, DevBuf& d, cudaStream_t st, 
     d.p = const_cast<void*>(src);
     return MGPU_OK;
   }
-  CK(cudaMalloc(&d.p, bytes));
-  d.owned = true;
+  int rc = alloc_on_stream(d, bytes, st);
+  if (rc) return rc;
   if (copy) CK(cudaMemcpyAsync(d.p, src, bytes, cudaMemcpyHostToDevice, st));
   return MGPU_OK;
 }
@@ -882,25 +900,26 @@ static int run_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* seeds, const u
   std::vector<CellTask> tasks(ncells);
   std::vector<uint64_t> hs(ncells), ht(ncells);
   const bool seeds_dev = is_device_ptr(seeds), targets_dev = is_device_ptr(targets);
-  if (seeds_dev) CK(cudaMemcpy(hs.data(), seeds, ncells * 8, cudaMemcpyDeviceToHost));
-  if (targets_dev) CK(cudaMemcpy(ht.data(), targets, ncells * 8, cudaMemcpyDeviceToHost));
+  if (seeds_dev) CK(cudaMemcpyAsync(hs.data(), seeds, ncells * 8, cudaMemcpyDeviceToHost, st));
+  if (targets_dev) CK(cudaMemcpyAsync(ht.data(), targets, ncells * 8, cudaMemcpyDeviceToHost, st));
+  if (seeds_dev || targets_dev) CK(cudaStreamSynchronize(st));
   for (uint64_t i = 0; i < ncells; ++i) {
     tasks[i].seed = seeds_dev ? hs[i] : seeds[i];
     tasks[i].target_contacts = targets_dev ? ht[i] : targets[i];
   }
   DevBuf d_tasks;
-  CK(cudaMalloc(&d_tasks.p, ncells * sizeof(CellTask)));
-  d_tasks.owned = true;
+  rc = alloc_on_stream(d_tasks, ncells * sizeof(CellTask), st);
+  if (rc) return rc;
   CK(cudaMemcpyAsync(d_tasks.p, tasks.data(), ncells * sizeof(CellTask), cudaMemcpyHostToDevice, st));
   const size_t band_bytes = (size_t)P.nrows * P.ncols * sizeof(uint32_t);
   DevBuf d_band, d_missed, d_stats;
   rc = to_device(band, band_bytes, d_band, st, true);
   if (rc) return rc;
-  CK(cudaMalloc(&d_missed.p, 8));
-  d_missed.owned = true;
+  rc = alloc_on_stream(d_missed, 8, st);
+  if (rc) return rc;
   CK(cudaMemsetAsync(d_missed.p, 0, 8, st));
-  CK(cudaMalloc(&d_stats.p, ncells * sizeof(mgpu_cell_stats)));
-  d_stats.owned = true;
+  rc = alloc_on_stream(d_stats, ncells * sizeof(mgpu_cell_stats), st);
+  if (rc) return rc;
   char err[256] = {0};
   DevChrom dc{ch.d_bars, ch.nb};
   if (P.slot_bytes) {
@@ -930,16 +949,19 @@ static int run_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* seeds, const u
   if (missed) {
     if (is_device_ptr(missed)) {
       uint64_t cur = 0;
-      CK(cudaMemcpy(&cur, missed, 8, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpyAsync(&cur, missed, 8, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
       cur += h_missed;
-      CK(cudaMemcpy(missed, &cur, 8, cudaMemcpyHostToDevice));
+      CK(cudaMemcpyAsync(missed, &cur, 8, cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
     } else {
       *missed += h_missed;
     }
   }
   if (stats) {
     if (is_device_ptr(stats)) {
-      CK(cudaMemcpy(stats, h_stats.data(), ncells * sizeof(mgpu_cell_stats), cudaMemcpyHostToDevice));
+      CK(cudaMemcpyAsync(stats, h_stats.data(), ncells * sizeof(mgpu_cell_stats), cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
     } else {
       std::memcpy(stats, h_stats.data(), ncells * sizeof(mgpu_cell_stats));
     }

@@ -43,21 +43,57 @@ def prepare_chrom(eng, cfg, chrom, barriers, ncells):
                 seeds=seeds, nrows=nrows, ncols=ncols)
 
 
-def simulate_genome(cfg, genome, ncells=None, device=0, simulate_wo_barriers=False):
-    """Run every cell of every chromosome; returns a list of ChromResult."""
-    ncells = int(cfg.num_cells if ncells is None else ncells)
-    out = []
-    with engine.Engine(cfg, device) as eng:
-        for chrom, barriers in genome:
-            if not barriers and not simulate_wo_barriers:
-                continue
-            t = prepare_chrom(eng, cfg, chrom, barriers, ncells)
-            band = np.zeros(t["nrows"] * t["ncols"], dtype=np.uint32)
-            missed, stats = eng.simulate_cells(t["cid"], t["seeds"], t["targets"], t["target_epochs"],
-                                               t["nlefs"], band)
-            out.append(ChromResult(chrom, t["nlefs"], band, missed, stats))
-    return out
+# Shared-memory budget per cell when several chromosome launches run at once: enough for the
+# hottest per-LEF arrays of a mid-sized chromosome while four or more cells fit on an SM.
+CONCURRENT_SMEM_BUDGET = 48 * 1024
 
+
+def simulate_genome(cfg, genome, ncells=None, device=0, simulate_wo_barriers=False, workers=1,
+                    smem_budget=None):
+    """Run every cell of every chromosome; returns a list of ChromResult in genome order.
+
+    With ``workers`` > 1, that many host threads each drive their own engine context (own
+    CUDA stream), taking chromosomes from a queue largest first, so several one-chromosome
+    launches share the GPU at once, as the reference's worker threads share its cores.
+    ``smem_budget`` caps each cell's shared memory (bytes; default: the device limit with one
+    worker, CONCURRENT_SMEM_BUDGET with several)."""
+    import queue
+    import threading
+
+    ncells = int(cfg.num_cells if ncells is None else ncells)
+    jobs = [(i, c, b) for i, (c, b) in enumerate(genome) if b or simulate_wo_barriers]
+    if smem_budget is None:
+        smem_budget = 0 if workers <= 1 else CONCURRENT_SMEM_BUDGET
+    todo = queue.Queue()
+    for job in sorted(jobs, key=lambda j: -j[1].simulated_size):
+        todo.put(job)
+    results, errors = {}, []
+
+    def worker():
+        try:
+            with engine.Engine(cfg, device) as eng:
+                eng.set_debug_flags(0, smem_budget)
+                while True:
+                    try:
+                        i, chrom, barriers = todo.get_nowait()
+                    except queue.Empty:
+                        return
+                    t = prepare_chrom(eng, cfg, chrom, barriers, ncells)
+                    band = np.zeros(t["nrows"] * t["ncols"], dtype=np.uint32)
+                    missed, stats = eng.simulate_cells(t["cid"], t["seeds"], t["targets"],
+                                                       t["target_epochs"], t["nlefs"], band)
+                    results[i] = ChromResult(chrom, t["nlefs"], band, missed, stats)
+        except BaseException as e:  # surfaced to the caller below
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker) for _ in range(max(1, workers))]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    if errors:
+        raise errors[0]
+    return [results[i] for i, _, _ in jobs]
 
 def _main(argv=None):
     """Run one workload and print its throughput, e.g. for profiling one launch:
@@ -75,6 +111,8 @@ def _main(argv=None):
     ap.add_argument("--chrom", type=int, action="append", help="chromosome index (repeatable)")
     ap.add_argument("--cells", type=int, default=None)
     ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--workers", type=int, default=1, help="concurrent chromosome launches")
+    ap.add_argument("--smem-budget", type=int, default=None, help="shared memory per cell (bytes)")
     args = ap.parse_args(argv)
     cfg, g = gen.parity_10mbp() if args.workload == "parity" else gen.genome_24chr()
     if args.chrom:
@@ -82,11 +120,11 @@ def _main(argv=None):
     if args.cells is not None:
         cfg.num_cells = args.cells
     t0 = time.perf_counter()
-    res = simulate_genome(cfg, g, device=args.device)
+    res = simulate_genome(cfg, g, device=args.device, workers=args.workers, smem_budget=args.smem_budget)
     dt = time.perf_counter() - t0
     le = sum(r.lef_epochs for r in res)
     print(json.dumps({"workload": args.workload, "chromosomes": [r.chrom.name for r in res],
-                      "cells": int(cfg.num_cells), "lef_epochs": le, "contacts": sum(r.contacts for r in res),
+                      "cells": int(cfg.num_cells), "workers": args.workers, "lef_epochs": le, "contacts": sum(r.contacts for r in res),
                       "wall_s": dt, "lef_epochs_per_s": le / dt}))
 
 

@@ -218,6 +218,23 @@ def test_host_buffers_accumulate_into_band():
     assert np.array_equal(band, 2 * once)
 
 
+def test_concurrent_contexts_match_one_context():
+    """Chromosome launches from several contexts at once (threads, streams, a shared-memory
+    budget that moves arrays to global slots) give the same bands and cells as one context."""
+    from modlefork_gb300 import simulate
+
+    cfg, gen = genome.genome_24chr(seed=5, nchroms=4, min_len=2_000_000, max_len=6_000_000)
+    cfg.num_cells = 16
+    one = simulate.simulate_genome(cfg, gen, workers=1)
+    many = simulate.simulate_genome(cfg, gen, workers=3, smem_budget=12 * 1024)
+    assert [r.chrom.name for r in one] == [r.chrom.name for r in many]
+    for a, b in zip(one, many):
+        assert np.array_equal(a.band, b.band), a.chrom.name
+        assert a.missed == b.missed
+        assert [(s.epochs, s.contacts, s.rng_draws) for s in a.stats] == \
+               [(s.epochs, s.contacts, s.rng_draws) for s in b.stats]
+
+
 def test_device_buffers_match_host_buffers():
     """Seeds, targets and band given as device pointers (torch tensors) give the same band
     and statistics as host arrays, on a caller's stream."""
