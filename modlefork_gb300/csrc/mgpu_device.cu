@@ -114,11 +114,17 @@ struct Cell {
   u32* bst;
   double *hcfx, *havg;
   const DevBarrier* bar;
+  const uint2* bpf;  // {pos, flags}
   u32 nb;
   u32 nl;
   const ulonglong2* jt;
   u32* band;
 };
+
+// Position and flags of barrier i through the read-only data path (8 bytes per barrier, so the
+// sweeps over the barrier track stay in cache).
+__device__ __forceinline__ u32 bar_pos(const Cell& c, u32 i) { return __ldg(&c.bpf[i].x); }
+__device__ __forceinline__ u32 bar_flags(const Cell& c, u32 i) { return __ldg(&c.bpf[i].y); }
 
 // ---------------------------------------------------------------------------------------
 // PRNG ring
@@ -711,9 +717,9 @@ __device__ void detect_lef_bar_serial(Cell& c, const KParams& P, u32 n, u64 n5, 
   bool rev_done = false;
   for (u32 i = 0; i < c.nb && !rev_done; ++i) {
     if (!bar_active(c, i)) continue;
-    const u32 dir = c.bar[i].flags & BF_DIR_MASK;
+    const u32 dir = bar_flags(c, i) & BF_DIR_MASK;
     const Trial& tr = P.lef_bar[dir == MGPU_DIR_REV ? 0 : 1];
-    const u64 bpos = c.bar[i].pos;
+    const u64 bpos = bar_pos(c, i);
     while (unit_pos <= bpos) {
       if (++j == n) {
         rev_done = true;
@@ -735,9 +741,9 @@ __device__ void detect_lef_bar_serial(Cell& c, const KParams& P, u32 n, u64 n5, 
   unit_pos = pos64(c.fwd[unit_idx]);
   for (u64 i = (u64)c.nb - 1; i != ~0ull; --i) {
     if (!bar_active(c, (u32)i)) continue;
-    const u32 dir = c.bar[i].flags & BF_DIR_MASK;
+    const u32 dir = bar_flags(c, i) & BF_DIR_MASK;
     const Trial& tr = P.lef_bar[dir == MGPU_DIR_FWD ? 0 : 1];
-    const u64 bpos = c.bar[i].pos;
+    const u64 bpos = bar_pos(c, i);
     while (unit_pos >= bpos) {
       if (--j == ~0ull) return;
       unit_idx = c.fr[j];
@@ -757,7 +763,7 @@ __device__ __forceinline__ u64 barrier_pos_checked(Cell& c, u32 idx) {
     set_status(c, DEV_ERR_BAD_STATE);
     return 0;
   }
-  return c.bar[idx].pos;
+  return bar_pos(c, idx);
 }
 
 // The collision words of one tested primary pair (simulation_detect_collisions.cpp:344-399).
@@ -922,7 +928,7 @@ __device__ void barriers_init(Cell& c, u64* s) {
   for (u32 base = 0; base < c.nb; base += 32) {
     rng_ensure(c, s, 32);
     const u32 i = base + ln();
-    const bool need = i < c.nb && (c.bar[i].flags & BF_OCC_DRAWS);
+    const bool need = i < c.nb && (bar_flags(c, i) & BF_OCC_DRAWS);
     const unsigned m = __ballot_sync(FULL, need);
     const u32 off = __popc(m & lanemask_lt());
     bool occ = false;
@@ -946,7 +952,7 @@ __device__ void barriers_next(Cell& c, u64* s) {
     bool st = (c.bst[base >> 5] >> ln()) & 1u;
     if (valid) {
       const u64 u = ring_at(c, c.sc->rpos + ln());
-      const u32 f = c.bar[i].flags;
+      const u32 f = bar_flags(c, i);
       if (!st) {
         st = !(f & BF_INA_NEVER) && u >= c.bar[i].t_ina;
       } else {
@@ -1222,17 +1228,10 @@ __device__ bool rank_dir_split(Cell& c, u32 dir, u32 n) {
       __syncwarp();
     }
   }
-  // merge: K first among equal keys
-  for (u32 i = lane; i < ns; i += 32) {
-    const u32 idx = K[i];
-    const u64 key = rank_key(c, dir, idx);
-    u32 lo = 0, hi = kE;
-    while (lo < hi) {
-      const u32 mid = (lo + hi) >> 1;
-      if (rank_key(c, dir, Bf[mid]) < key) lo = mid + 1; else hi = mid;
-    }
-    R[i + lo] = idx;
-  }
+  // merge, K first among equal keys.  u_j = #K with key <= key(B_j) (binary search; K is
+  // sorted by key), so B_j lands at j + u_j and K_i at i + #{j : u_j <= i}; u is
+  // non-decreasing in j, so one pass over K with a pointer into u counts the latter.
+  u32* U = Bf == Bs ? B : Bs;  // the dead one of the two B buffers
   for (u32 j = lane; j < kE; j += 32) {
     const u32 idx = Bf[j];
     const u64 key = rank_key(c, dir, idx);
@@ -1241,7 +1240,21 @@ __device__ bool rank_dir_split(Cell& c, u32 dir, u32 n) {
       const u32 mid = (lo + hi) >> 1;
       if (rank_key(c, dir, K[mid]) <= key) lo = mid + 1; else hi = mid;
     }
+    U[j] = lo;
     R[j + lo] = idx;
+  }
+  __syncwarp();
+  u32 jb = 0;  // B elements with u_j below the chunk
+  for (u32 base = 0; base < ns; base += 32) {
+    const u32 i = base + lane;
+    u32 cnt = jb, j = jb;
+    for (; j < kE; ++j) {
+      const u32 uj = U[j];
+      if (uj >= base + 32) break;
+      cnt += uj <= i ? 1u : 0u;
+    }
+    if (i < ns) R[i + cnt] = K[i];
+    jb = j;
   }
   __syncwarp();
   return true;
@@ -1481,6 +1494,63 @@ __device__ bool ranked_sorted(const Cell& c, u32 n) {
   return !__any_sync(FULL, bad);
 }
 
+// Bucket index over a sorted array of ranked positions (unbound units, UNBOUND, at the tail):
+// T[b] = #{k : key[k] < start + (b << shift)} for b in [0, nbk], with shift chosen so that
+// nbk + 1 <= n (about one key per bucket).  lower_bound(x) then starts from T[b(x)] and scans a
+// few keys instead of a binary search over the whole array.
+struct BucketIndex {
+  const u32* key;
+  const u32* T;
+  u32 n, start, shift, nbk;
+  __device__ u32 lower_bound(u32 x) const {
+    if (x <= start) return 0;
+    u32 b = (x - start) >> shift;
+    if (b > nbk) b = nbk;
+    u32 k = T[b];
+    while (k < n && key[k] < x) ++k;
+    return k;
+  }
+};
+
+// Collective; T needs n entries.  Returns an index with T == nullptr (binary-search fallback)
+// when n is too small for a table.
+__device__ BucketIndex build_bucket_index(const u32* key, u32 n, u32 start, u32 end, u32* T) {
+  BucketIndex ix{key, nullptr, n, start, 0, 0};
+  if (n < 8 || end <= start) return ix;
+  const u32 range = end - start;
+  u32 shift = 0;
+  while ((range >> shift) + 2 > n) ++shift;
+  const u32 nbk = range >> shift;
+  for (u32 k = ln(); k <= n; k += 32) {
+    u32 bmin = 0, bmax = nbk;
+    if (k > 0) {
+      const u32 lo = key[k - 1];
+      bmin = lo == UNBOUND ? nbk + 1 : ((lo - start) >> shift) + 1;
+    }
+    if (k < n) {
+      const u32 hi = key[k];
+      if (hi != UNBOUND) bmax = min(nbk, (hi - start) >> shift);
+    }
+    for (u32 b = bmin; b <= bmax; ++b) T[b] = k;
+  }
+  __syncwarp();
+  ix.T = T;
+  ix.shift = shift;
+  ix.nbk = nbk;
+  return ix;
+}
+
+// first k in [0, n) with key[k] >= x
+__device__ __forceinline__ u32 ranked_lower_bound(const BucketIndex& ix, u32 x) {
+  if (ix.T) return ix.lower_bound(x);
+  u32 lo = 0, hi = ix.n;
+  while (lo < hi) {
+    const u32 mid = (lo + hi) >> 1;
+    if (ix.key[mid] >= x) hi = mid; else lo = mid + 1;
+  }
+  return lo;
+}
+
 // Bernoulli trial of one lane with the draw at its offset (or none).
 __device__ __forceinline__ bool trial_needs_draw(const Trial& t) { return !t.always && t.draws; }
 __device__ __forceinline__ bool trial_outcome(const Trial& t, u64 u) {
@@ -1497,23 +1567,20 @@ __device__ __forceinline__ bool trial_outcome(const Trial& t, u64 u) {
 // hit by several barriers keeps the last successful one in that order.
 __device__ void detect_lef_bar_fast(Cell& c, u64* s, const KParams& P, u32 n, u64 n5, u64 n3) {
   const u32 j0 = (u32)min(n5, n5 - 1);
+  const BucketIndex ixr = build_bucket_index(c.sr, n, (u32)P.start, (u32)P.end, c.tmp);
   for (u32 base = 0; base < c.nb; base += 32) {
     rng_ensure(c, s, 32);
     const u32 i = base + ln();
     bool cand = false, drawn = false;
     u32 unit = 0;
     if (i < c.nb && bar_active(c, i)) {
-      const u32 bpos = c.bar[i].pos;
-      u32 lo = j0, hi = n;  // first k in [j0, n) with sr[k] > bpos
-      while (lo < hi) {
-        const u32 mid = (lo + hi) >> 1;
-        if (c.sr[mid] > bpos) hi = mid; else lo = mid + 1;
-      }
+      const u32 bpos = bar_pos(c, i);
+      const u32 lo = max(j0, ranked_lower_bound(ixr, bpos + 1));  // first k >= j0 with sr[k] > bpos
       if (lo < n) {
         unit = c.rr[lo];
         if (c.bep[unit] != UNBOUND) {
           const u64 delta = (u64)c.sr[lo] - bpos;
-          const Trial& tr = P.lef_bar[(c.bar[i].flags & BF_DIR_MASK) == MGPU_DIR_REV ? 0 : 1];
+          const Trial& tr = P.lef_bar[(bar_flags(c, i) & BF_DIR_MASK) == MGPU_DIR_REV ? 0 : 1];
           if (delta > 0 && delta <= c.rm[unit]) {
             cand = true;
             drawn = trial_needs_draw(tr);
@@ -1524,7 +1591,7 @@ __device__ void detect_lef_bar_fast(Cell& c, u64* s, const KParams& P, u32 n, u6
     const unsigned dm = __ballot_sync(FULL, drawn);
     bool hit = false;
     if (cand) {
-      const Trial& tr = P.lef_bar[(c.bar[i].flags & BF_DIR_MASK) == MGPU_DIR_REV ? 0 : 1];
+      const Trial& tr = P.lef_bar[(bar_flags(c, i) & BF_DIR_MASK) == MGPU_DIR_REV ? 0 : 1];
       const u64 u = drawn ? ring_at(c, c.sc->rpos + __popc(dm & lanemask_lt())) : 0;
       hit = trial_outcome(tr, u);
     }
@@ -1537,24 +1604,21 @@ __device__ void detect_lef_bar_fast(Cell& c, u64* s, const KParams& P, u32 n, u6
     __syncwarp();
   }
   const u32 jtop = (u32)(n - min(n3, n3 - 1)) - 1;  // last fwd rank index searched
+  const BucketIndex ixf = build_bucket_index(c.sf, n, (u32)P.start, (u32)P.end, c.tmp);
   for (i64 top = (i64)c.nb - 1; top >= 0; top -= 32) {
     rng_ensure(c, s, 32);
     const i64 ii = top - (i64)ln();
     bool cand = false, drawn = false;
     u32 unit = 0;
     if (ii >= 0 && bar_active(c, (u32)ii)) {
-      const u32 bpos = c.bar[ii].pos;
-      u32 lo = 0, hi = jtop + 1;  // first k in [0, jtop] with sf[k] >= bpos
-      while (lo < hi) {
-        const u32 mid = (lo + hi) >> 1;
-        if (c.sf[mid] >= bpos) hi = mid; else lo = mid + 1;
-      }
+      const u32 bpos = bar_pos(c, ii);
+      const u32 lo = min(jtop + 1, ranked_lower_bound(ixf, bpos));  // first k <= jtop with sf[k] >= bpos
       if (lo > 0) {
         const u32 k = lo - 1;
         unit = c.fr[k];
         if (c.bep[unit] != UNBOUND) {
           const u64 delta = (u64)bpos - c.sf[k];
-          const Trial& tr = P.lef_bar[(c.bar[ii].flags & BF_DIR_MASK) == MGPU_DIR_FWD ? 0 : 1];
+          const Trial& tr = P.lef_bar[(bar_flags(c, ii) & BF_DIR_MASK) == MGPU_DIR_FWD ? 0 : 1];
           if (delta > 0 && delta <= c.fm[unit]) {
             cand = true;
             drawn = trial_needs_draw(tr);
@@ -1565,7 +1629,7 @@ __device__ void detect_lef_bar_fast(Cell& c, u64* s, const KParams& P, u32 n, u6
     const unsigned dm = __ballot_sync(FULL, drawn);
     bool hit = false;
     if (cand) {
-      const Trial& tr = P.lef_bar[(c.bar[ii].flags & BF_DIR_MASK) == MGPU_DIR_FWD ? 0 : 1];
+      const Trial& tr = P.lef_bar[(bar_flags(c, ii) & BF_DIR_MASK) == MGPU_DIR_FWD ? 0 : 1];
       const u64 u = drawn ? ring_at(c, c.sc->rpos + __popc(dm & lanemask_lt())) : 0;
       hit = trial_outcome(tr, u);
     }
@@ -1587,21 +1651,15 @@ __device__ void detect_lef_bar_fast(Cell& c, u64* s, const KParams& P, u32 n, u6
 __device__ void detect_primary_fast(Cell& c, u64* s, const KParams& P, u32 n, u64 n5, u64 n3) {
   if (n5 == n || n3 == n) return;
   const u32 i2 = (u32)(n - min(n3, n3 - 1));
+  // bucket index over the fwd ranked positions (this step can also run on its own)
+  const BucketIndex ixf = build_bucket_index(c.sf, n, (u32)P.start, (u32)P.end, c.tmp);
   u32 carry = 0;  // cnt of the element before the chunk
   for (u32 base = (u32)n5; base < n; base += 32) {
     rng_ensure(c, s, 32);
     const u32 j = base + ln();
     const bool valid = j < n;
     u32 cnt = 0;
-    if (valid) {
-      const u32 rp = c.sr[j];
-      u32 lo = 0, hi = i2;  // first i in [0, i2) with sf[i] >= rp
-      while (lo < hi) {
-        const u32 mid = (lo + hi) >> 1;
-        if (c.sf[mid] >= rp) hi = mid; else lo = mid + 1;
-      }
-      cnt = lo;
-    }
+    if (valid) cnt = min(i2, ranked_lower_bound(ixf, c.sr[j]));  // first i < i2 with sf[i] >= rp
     u32 prev = __shfl_up_sync(FULL, cnt, 1);
     if (ln() == 0) prev = carry;
     const bool tested = valid && cnt > prev && cnt < i2;
@@ -1634,8 +1692,8 @@ __device__ void detect_primary_fast(Cell& c, u64* s, const KParams& P, u32 n, u6
 __device__ void correct_lef_bar(Cell& c, u32 n) {
   for (u32 i = ln(); i < n; i += 32) {
     const u32 r = c.rc[i], f = c.fc[i];
-    if (cw_occurred_as(r, EV_LEF_BAR)) c.rm[i] = (u32)(pos64(c.rev[i]) - c.bar[cw_idx(r)].pos - 1);
-    if (cw_occurred_as(f, EV_LEF_BAR)) c.fm[i] = (u32)(c.bar[cw_idx(f)].pos - pos64(c.fwd[i]) - 1);
+    if (cw_occurred_as(r, EV_LEF_BAR)) c.rm[i] = (u32)(pos64(c.rev[i]) - bar_pos(c, cw_idx(r)) - 1);
+    if (cw_occurred_as(f, EV_LEF_BAR)) c.fm[i] = (u32)(bar_pos(c, cw_idx(f)) - pos64(c.fwd[i]) - 1);
   }
   __syncwarp();
 }
@@ -1643,8 +1701,9 @@ __device__ void correct_lef_bar(Cell& c, u32 n) {
 // correct_moves_for_primary_lef_lef_collisions (simulation_correct_moves.cpp:54-122): the
 // pairs it visits are disjoint, so both passes are warp-parallel.
 __device__ void correct_primary(Cell& c, u32 n) {
-  for (u32 k = ln(); k < n; k += 32) {
-    const u32 rev_idx = c.rr[k];
+  // detect_primary pairs each fwd unit with at most one rev unit, so visiting the units in
+  // index order instead of rank order changes nothing
+  for (u32 rev_idx = ln(); rev_idx < n; rev_idx += 32) {
     const u32 r = c.rc[rev_idx];
     if (!cw_occurred_as(r, EV_PRIMARY)) continue;
     const u32 fwd_idx = cw_idx(r);
@@ -1660,8 +1719,7 @@ __device__ void correct_primary(Cell& c, u32 n) {
     }
   }
   __syncwarp();
-  for (u32 k = ln(); k < n; k += 32) {
-    const u32 fwd_idx = c.fr[k];
+  for (u32 fwd_idx = ln(); fwd_idx < n; fwd_idx += 32) {
     const u32 f = c.fc[fwd_idx];
     if (!cw_occurred_as(f, EV_PRIMARY)) continue;
     const u32 rev_idx = cw_idx(f);
@@ -1915,8 +1973,8 @@ __device__ u32 release_lefs(Cell& c, u64* s, const KParams& P, u32 n, bool compl
     if (bound) {
       const u32 r = c.rc[i], f = c.fc[i];
       u32 nh = 0;
-      if (cw_occurred_as(r, EV_LEF_BAR) && (c.bar[cw_idx(r)].flags & BF_DIR_MASK) == MGPU_DIR_REV) ++nh;
-      if (cw_occurred_as(f, EV_LEF_BAR) && (c.bar[cw_idx(f)].flags & BF_DIR_MASK) == MGPU_DIR_FWD) ++nh;
+      if (cw_occurred_as(r, EV_LEF_BAR) && (bar_flags(c, cw_idx(r)) & BF_DIR_MASK) == MGPU_DIR_REV) ++nh;
+      if (cw_occurred_as(f, EV_LEF_BAR) && (bar_flags(c, cw_idx(f)) & BF_DIR_MASK) == MGPU_DIR_FWD) ++nh;
       tr = P.release[completed ? 1 : 0][nh];
     }
     const bool need = bound && tr.draws;
@@ -2354,6 +2412,7 @@ __device__ void carve(Cell& c, char* smem, char* gslot, const KParams& P, u32 nl
       *arr[k] = reinterpret_cast<u32*>(base + P.arr_off[k]);
     }
     c.bar = ch.barriers;
+    c.bpf = ch.pos_flags;
     c.nb = ch.nbarriers;
     c.nl = nl;
     c.jt = jt;
@@ -2705,11 +2764,18 @@ static int cuda_fail(cudaError_t e, const char* what, char* errbuf, int errlen) 
   return MGPU_ERR_CUDA;
 }
 
+// Largest dynamic shared memory a block of either kernel may request: the device's opt-in
+// limit minus the kernels' static shared memory.
 u64 max_smem_per_block() {
   int dev = 0, v = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  return (u64)v;
+  u64 stat = 0;
+  cudaFuncAttributes a{};
+  if (cudaFuncGetAttributes(&a, simulate_kernel) == cudaSuccess) stat = a.sharedSizeBytes;
+  if (cudaFuncGetAttributes(&a, phase_kernel) == cudaSuccess && a.sharedSizeBytes > stat) stat = a.sharedSizeBytes;
+  cudaGetLastError();
+  return (u64)v > stat ? (u64)v - stat : 0;
 }
 
 u64 resident_cells(const KParams& P, u64 ncells) {

@@ -538,6 +538,7 @@ struct ChromEntry {
   mgpu_chrom chrom{};
   std::string name;
   DevBarrier* d_bars = nullptr;
+  uint2* d_pos_flags = nullptr;  // inside the d_bars allocation
   u32 nb = 0;
 };
 
@@ -676,8 +677,14 @@ extern "C" int mgpu_upload_chrom(mgpu_ctx* ctx, const mgpu_chrom* chrom, const m
   e.chrom = *chrom;
   e.nb = (u32)nb;
   if (nb) {
-    CK(cudaMalloc(&e.d_bars, nb * sizeof(DevBarrier)));
+    // one allocation: the DevBarrier records, then the compact {pos, flags} pairs
+    std::vector<uint2> pf(nb);
+    for (uint64_t i = 0; i < nb; ++i) pf[i] = make_uint2(dev[i].pos, dev[i].flags);
+    const size_t rec_bytes = (nb * sizeof(DevBarrier) + 15) & ~size_t(15);
+    CK(cudaMalloc(&e.d_bars, rec_bytes + nb * sizeof(uint2)));
     CK(cudaMemcpy(e.d_bars, dev.data(), nb * sizeof(DevBarrier), cudaMemcpyHostToDevice));
+    e.d_pos_flags = reinterpret_cast<uint2*>(reinterpret_cast<char*>(e.d_bars) + rec_bytes);
+    CK(cudaMemcpy(e.d_pos_flags, pf.data(), nb * sizeof(uint2), cudaMemcpyHostToDevice));
   }
   ctx->chroms.push_back(e);
   *chrom_id = (int)ctx->chroms.size() - 1;
@@ -921,7 +928,7 @@ static int run_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* seeds, const u
   rc = alloc_on_stream(d_stats, ncells * sizeof(mgpu_cell_stats), st);
   if (rc) return rc;
   char err[256] = {0};
-  DevChrom dc{ch.d_bars, ch.nb};
+  DevChrom dc{ch.d_bars, ch.d_pos_flags, ch.nb};
   if (P.slot_bytes) {
     rc = ensure_scratch(ctx, P, resident_cells(P, ncells));
     if (rc) return rc;
@@ -1041,7 +1048,7 @@ extern "C" int mgpu_simulate_cells_noalloc(mgpu_ctx* ctx, int chrom_id, const ui
   CellTask* tasks = (CellTask*)(scratch + NOALLOC_TASKS_OFFSET);
   rc = launch_pack_tasks(cell_seeds, target_contacts, ncells, tasks, st, err, sizeof(err));
   if (rc) return fail(rc, "%s", err);
-  DevChrom dc{ch.d_bars, ch.nb};
+  DevChrom dc{ch.d_bars, ch.d_pos_flags, ch.nb};
   rc = launch_simulate(P, dc, tasks, ncells, target_epochs, band, missed_updates, stats, nullptr,
                        ctx->d_jump, (u32*)scratch, scratch + NOALLOC_SLOTS_OFFSET, slot_room, st, err,
                        sizeof(err));
@@ -1176,7 +1183,7 @@ extern "C" int mgpu_run_phase(mgpu_ctx* ctx, int chrom_id, int phase, mgpu_phase
   d_outs.owned = true;
   CK(cudaMemset(d_outs.p, 0, 32));
   char err[256] = {0};
-  DevChrom dc{ch.d_bars, ch.nb};
+  DevChrom dc{ch.d_bars, ch.d_pos_flags, ch.nb};
   if (P.slot_bytes) {
     rc = ensure_scratch(ctx, P, 1);
     if (rc) return rc;

@@ -161,6 +161,7 @@ MGPU_HD inline u64 cell_header_bytes(u64 nbarriers, u64 hist_cap) {
 // Host side helpers implemented in mgpu_host.cpp, device launchers in mgpu_device.cu.
 struct DevChrom {
   const DevBarrier* barriers;
+  const uint2* pos_flags;  // {pos, flags} of each barrier: the compact copy the sweeps read
   u32 nbarriers;
 };
 

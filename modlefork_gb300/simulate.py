@@ -44,8 +44,8 @@ def prepare_chrom(eng, cfg, chrom, barriers, ncells):
 
 
 # Shared-memory budget per cell when several chromosome launches run at once: enough for the
-# hottest per-LEF arrays of a mid-sized chromosome while four or more cells fit on an SM.
-CONCURRENT_SMEM_BUDGET = 48 * 1024
+# hottest per-LEF arrays of a mid-sized chromosome while about seven cells fit on an SM.
+CONCURRENT_SMEM_BUDGET = 32 * 1024
 
 
 def simulate_genome(cfg, genome, ncells=None, device=0, simulate_wo_barriers=False, workers=1,
