@@ -299,6 +299,20 @@ int mgpu_simulate_cells_noalloc(mgpu_ctx* ctx, int chrom_id, const uint64_t* cel
                                 uint64_t num_lefs, uint64_t ncells, uint32_t* band,
                                 uint64_t* missed_updates, mgpu_cell_stats* stats);
 
+/*
+ * Pixel table of a band, for writing a cooler (Cooler::write_or_append_cmatrix_to_file,
+ * src/libmodle_io/cooler_write_impl.hpp:275-316): for bin1 row i = 0..ncols-1 and bin2
+ * j = i..min(i + nrows, ncols) - 1, every non-zero count, in that order, as
+ * (bin_offset + i, bin_offset + j, count).  bin_offset is the genome-wide id of the band's
+ * first bin.  bin1_offset[i] receives the number of pixels before row i (ncols + 1 entries; the
+ * last is the total).  bin1, bin2 and count may be NULL to query the size; otherwise they need
+ * `capacity` entries, and a capacity below the total returns MGPU_ERR_OVERFLOW with *nnz set
+ * and no pixel written.  Buffers may be host or device pointers.
+ */
+int mgpu_band_to_pixels(mgpu_ctx* ctx, const uint32_t* band, uint64_t nrows, uint64_t ncols,
+                        uint64_t bin_offset, uint64_t* bin1_offset, int64_t* bin1, int64_t* bin2,
+                        uint32_t* count, uint64_t capacity, uint64_t* nnz);
+
 /* ---- parity and debugging entry points (used by the test-suite) ------------------------ */
 
 /*

@@ -14,7 +14,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libmgpu_modle.so")
-SOURCES = ["mgpu_device.cu", "mgpu_host.cpp"]
+SOURCES = ["mgpu_device.cu", "mgpu_pixels.cu", "mgpu_host.cpp"]
 HEADERS = ["mgpu_internal.h", "cppsort_emul.h", "ziggurat_tables.h",
            os.path.join("..", "..", "include", "mgpu_modle.h")]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
@@ -36,7 +36,7 @@ def _stale():
 
 
 def build(force=False, verbose=False):
-    """Compile the two translation units in parallel and link the shared library."""
+    """Compile the translation units in parallel and link the shared library."""
     if not force and not _stale():
         return LIB
     os.makedirs(LIBDIR, exist_ok=True)

@@ -987,6 +987,64 @@ extern "C" int mgpu_simulate_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* 
                    band, missed_updates, stats, nullptr);
 }
 
+// Copy a device result to the caller's buffer (host or device).
+static int copy_out(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  if (!dst || bytes == 0 || dst == src) return MGPU_OK;
+  CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, st));
+  return MGPU_OK;
+}
+
+extern "C" int mgpu_band_to_pixels(mgpu_ctx* ctx, const uint32_t* band, uint64_t nrows, uint64_t ncols,
+                                   uint64_t bin_offset, uint64_t* bin1_offset, int64_t* bin1,
+                                   int64_t* bin2, uint32_t* count, uint64_t capacity, uint64_t* nnz) {
+  if (!ctx || !nnz || !bin1_offset || (ncols && nrows && !band))
+    return fail(MGPU_ERR_INVALID_ARG, "mgpu_band_to_pixels: null argument");
+  const bool want_pixels = bin1 || bin2 || count;
+  if (want_pixels && !(bin1 && bin2 && count))
+    return fail(MGPU_ERR_INVALID_ARG, "mgpu_band_to_pixels: bin1, bin2 and count go together");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = active_stream(ctx);
+  const size_t band_bytes = (size_t)nrows * ncols * sizeof(uint32_t);
+  DevBuf d_band, d_counts, d_off;
+  int rc = to_device(band, band_bytes, d_band, st, true);
+  if (rc) return rc;
+  rc = alloc_on_stream(d_counts, (ncols ? ncols : 1) * sizeof(uint32_t), st);
+  if (rc) return rc;
+  rc = to_device(bin1_offset, (ncols + 1) * sizeof(uint64_t), d_off, st, false);
+  if (rc) return rc;
+  char err[256] = {0};
+  rc = launch_band_counts((const u32*)d_band.p, nrows, ncols, (u32*)d_counts.p, (u64*)d_off.p, st, err,
+                          sizeof(err));
+  if (rc) return fail(rc, "%s", err);
+  uint64_t total = 0;
+  CK(cudaMemcpyAsync(&total, (u64*)d_off.p + ncols, sizeof(total), cudaMemcpyDeviceToHost, st));
+  rc = copy_out(bin1_offset, d_off.p, (ncols + 1) * sizeof(uint64_t), st);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(st));
+  *nnz = total;
+  if (!want_pixels) return MGPU_OK;
+  if (capacity < total)
+    return fail(MGPU_ERR_OVERFLOW, "mgpu_band_to_pixels: capacity %llu < %llu non-zero pixels",
+                (unsigned long long)capacity, (unsigned long long)total);
+  DevBuf d_b1, d_b2, d_c;
+  rc = to_device(bin1, total * sizeof(int64_t), d_b1, st, false);
+  if (!rc) rc = to_device(bin2, total * sizeof(int64_t), d_b2, st, false);
+  if (!rc) rc = to_device(count, total * sizeof(uint32_t), d_c, st, false);
+  if (rc) return rc;
+  if (total) {
+    rc = launch_band_pixels((const u32*)d_band.p, nrows, ncols, bin_offset, (const u64*)d_off.p,
+                            (int64_t*)d_b1.p, (int64_t*)d_b2.p, (u32*)d_c.p, st, err, sizeof(err));
+    if (rc) return fail(rc, "%s", err);
+    rc = copy_out(bin1, d_b1.p, total * sizeof(int64_t), st);
+    if (!rc) rc = copy_out(bin2, d_b2.p, total * sizeof(int64_t), st);
+    if (!rc) rc = copy_out(count, d_c.p, total * sizeof(uint32_t), st);
+    if (rc) return rc;
+  }
+  CK(cudaStreamSynchronize(st));
+  return MGPU_OK;
+}
+
 // Address of the fixed scratch, looked up once per device (with that device current).
 static std::mutex g_noalloc_mu;
 static constexpr int NOALLOC_MAX_DEVICES = 64;

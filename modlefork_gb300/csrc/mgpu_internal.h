@@ -183,6 +183,13 @@ constexpr u64 NOALLOC_TASKS_OFFSET = 256;
 constexpr u64 NOALLOC_SLOTS_OFFSET =
     (NOALLOC_TASKS_OFFSET + (u64)MGPU_NOALLOC_MAX_CELLS * sizeof(CellTask) + 255) & ~255ull;
 static_assert(NOALLOC_SLOTS_OFFSET < MGPU_NOALLOC_SCRATCH_BYTES, "task list larger than the scratch");
+// Pixel table of a band (mgpu_pixels.cu): counts[i] = non-zero pixels of bin1 row i,
+// offsets[0..ncols] their exclusive scan; then the (bin1, bin2, count) pixels.
+int launch_band_counts(const u32* band, u64 nrows, u64 ncols, u32* counts, u64* offsets, void* stream,
+                       char* errbuf, int errlen);
+int launch_band_pixels(const u32* band, u64 nrows, u64 ncols, u64 bin_offset, const u64* offsets,
+                       int64_t* bin1, int64_t* bin2, u32* count, void* stream, char* errbuf, int errlen);
+
 // Address of the scratch on the current device.
 int noalloc_scratch_address(void** ptr, char* errbuf, int errlen);
 // tasks[i] = {seeds[i], targets[i]} on the stream.

@@ -59,6 +59,8 @@ def load(path=LIB_PATH):
                                       C.c_void_p, C.c_void_p, C.c_void_p]),
         "mgpu_simulate_cells_noalloc": (i32, [C.c_void_p, i32, C.c_void_p, C.c_void_p, u64, u64, u64,
                                               C.c_void_p, C.c_void_p, C.c_void_p]),
+        "mgpu_band_to_pixels": (i32, [C.c_void_p, C.c_void_p, u64, u64, u64, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, u64, P(u64)]),
         "mgpu_trace_cell": (i32, [C.c_void_p, i32, u64, u64, u64, u64, C.c_void_p,
                                   P(abi.CellStats), P(abi.TraceRequest)]),
         "mgpu_state_digest": (u64, [u64] + [P(u64)] * 9),
@@ -243,6 +245,26 @@ class Engine:
                                             C.addressof(missed), C.addressof(st) if st else None),
                "mgpu_simulate_cells")
         return missed.value, st
+
+    def band_to_pixels(self, band, nrows, ncols, bin_offset=0):
+        """mgpu_band_to_pixels on a host uint32 band: returns (bin1_offset, bin1, bin2, count)
+        numpy arrays, the pixel table in the order a cooler file stores it."""
+        band = np.ascontiguousarray(band, dtype=np.uint32)
+        if band.size != nrows * ncols:
+            raise ValueError("band must hold nrows * ncols counts")
+        offs = np.zeros(ncols + 1, dtype=np.uint64)
+        nnz = C.c_uint64()
+        _check(self.lib.mgpu_band_to_pixels(self.h, band.ctypes.data, nrows, ncols, bin_offset, offs.ctypes.data,
+                                            None, None, None, 0, C.byref(nnz)), "mgpu_band_to_pixels")
+        n = nnz.value
+        b1 = np.zeros(n, dtype=np.int64)
+        b2 = np.zeros(n, dtype=np.int64)
+        cnt = np.zeros(n, dtype=np.uint32)
+        if n:
+            _check(self.lib.mgpu_band_to_pixels(self.h, band.ctypes.data, nrows, ncols, bin_offset,
+                                                offs.ctypes.data, b1.ctypes.data, b2.ctypes.data,
+                                                cnt.ctypes.data, n, C.byref(nnz)), "mgpu_band_to_pixels")
+        return offs, b1, b2, cnt
 
     def simulate_cells_noalloc(self, chrom_id, seeds_ptr, targets_ptr, target_epochs, nlefs, ncells,
                                band_ptr, missed_ptr=None, stats_ptr=None):

@@ -95,6 +95,33 @@ def simulate_genome(cfg, genome, ncells=None, device=0, simulate_wo_barriers=Fal
         raise errors[0]
     return [results[i] for i, _, _ in jobs]
 
+def genome_pixels(cfg, results, genome_chroms=None):
+    """Genome-wide pixel table of a run, as a cooler stores it (Cooler::write_or_append_cmatrix_to_file,
+    src/libmodle_io/cooler_write_impl.hpp:141-330): bins are numbered across the genome in
+    chromosome order, ceil(size / bin) per chromosome, and a band's first bin is its chromosome's
+    offset plus ceil(start / bin).  Returns (bin1, bin2, count) numpy arrays sorted by (bin1, bin2).
+
+    ``genome_chroms`` lists every chromosome of the genome in order (default: the simulated ones),
+    so that chromosomes skipped by the run still take their bins."""
+    chroms = genome_chroms if genome_chroms is not None else [r.chrom for r in results]
+    bin_size = int(cfg.bin_size)
+    first_bin, acc = {}, 0
+    for ch in chroms:
+        first_bin[ch.name] = acc
+        acc += (ch.size + bin_size - 1) // bin_size
+    b1s, b2s, cs = [], [], []
+    with engine.Engine(cfg) as eng:
+        for r in results:
+            nrows, ncols = engine.band_shape(cfg, r.chrom.simulated_size)
+            off = first_bin[r.chrom.name] + (r.chrom.start + bin_size - 1) // bin_size
+            _, b1, b2, c = eng.band_to_pixels(r.band, nrows, ncols, off)
+            b1s.append(b1)
+            b2s.append(b2)
+            cs.append(c)
+    cat = (lambda xs, dt: np.concatenate(xs) if xs else np.zeros(0, dt))
+    return cat(b1s, np.int64), cat(b2s, np.int64), cat(cs, np.uint32)
+
+
 def _main(argv=None):
     """Run one workload and print its throughput, e.g. for profiling one launch:
 
@@ -113,6 +140,7 @@ def _main(argv=None):
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--workers", type=int, default=1, help="concurrent chromosome launches")
     ap.add_argument("--smem-budget", type=int, default=None, help="shared memory per cell (bytes)")
+    ap.add_argument("--pixels", default=None, help="write the pixel table (bin1_id, bin2_id, count) as TSV")
     args = ap.parse_args(argv)
     cfg, g = gen.parity_10mbp() if args.workload == "parity" else gen.genome_24chr()
     if args.chrom:
@@ -122,6 +150,12 @@ def _main(argv=None):
     t0 = time.perf_counter()
     res = simulate_genome(cfg, g, device=args.device, workers=args.workers, smem_budget=args.smem_budget)
     dt = time.perf_counter() - t0
+    if args.pixels:
+        b1, b2, cnt = genome_pixels(cfg, res, [c for c, _ in g])
+        with open(args.pixels, "w") as f:
+            f.write("bin1_id\tbin2_id\tcount\n")
+            for a, b, c in zip(b1.tolist(), b2.tolist(), cnt.tolist()):
+                f.write(f"{a}\t{b}\t{c}\n")
     le = sum(r.lef_epochs for r in res)
     print(json.dumps({"workload": args.workload, "chromosomes": [r.chrom.name for r in res],
                       "cells": int(cfg.num_cells), "workers": args.workers, "lef_epochs": le, "contacts": sum(r.contacts for r in res),

@@ -1968,7 +1968,35 @@ int orc_run_phase(const mgpu_config* cfg, const mgpu_chrom* chrom, const mgpu_ba
   if (io->barrier_state)
     for (u64 i = 0; i < nb; ++i) io->barrier_state[i] = b.state[i];
   for (int k = 0; k < 4; ++k) io->prng_state[k] = g.s[k];
-  return ub ? MGPU_ERR_INTERNAL : MGPU_OK;
+    return ub ? MGPU_ERR_INTERNAL : MGPU_OK;
+}
+
+// Pixel table of one chromosome's band, in the order Cooler::write_or_append_cmatrix_to_file
+// emits it (src/libmodle_io/cooler_write_impl.hpp:275-316): bin1 i over the columns, bin2 j from i
+// to min(i + nrows, ncols) - 1, non-zero counts only, where the count of (i, j) is the band
+// entry at column j, row j - i (transpose_coords / encode_idx,
+// src/contact_matrix/contact_matrix_internal_impl.hpp:19-42).  bin1_offset[i] is the number of
+// pixels before row i (ncols + 1 entries).  Pixels are written only when capacity suffices.
+int orc_band_to_pixels(const uint32_t* band, uint64_t nrows, uint64_t ncols, uint64_t bin_offset,
+                       uint64_t* bin1_offset, int64_t* bin1, int64_t* bin2, uint32_t* count,
+                       uint64_t capacity, uint64_t* nnz) {
+  uint64_t k = 0;
+  for (uint64_t i = 0; i < ncols; ++i) {
+    bin1_offset[i] = k;
+    for (uint64_t j = i; j < i + nrows && j < ncols; ++j) {
+      const uint32_t m = band[j * nrows + (j - i)];
+      if (m == 0) continue;
+      if (k < capacity) {
+        bin1[k] = (int64_t)(bin_offset + i);
+        bin2[k] = (int64_t)(bin_offset + j);
+        count[k] = m;
+      }
+      ++k;
+    }
+  }
+  bin1_offset[ncols] = k;
+  *nnz = k;
+  return k <= capacity ? MGPU_OK : MGPU_ERR_OVERFLOW;
 }
 
 }  // extern "C"

@@ -60,8 +60,38 @@ def load_oracle():
     lib.orc_run_phase.argtypes = [P(abi.Config), P(abi.Chrom), P(abi.Barrier), C.c_uint64,
                                   C.c_int, P(abi.PhaseIO)]
     lib.orc_run_phase.restype = C.c_int
+    lib.orc_band_to_pixels.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, P(C.c_uint64)]
+    lib.orc_band_to_pixels.restype = C.c_int
     _oracle = lib
     return lib
+
+
+def oracle_pixels(band, nrows, ncols, bin_offset=0):
+    """The oracle's pixel table of a band: (bin1_offset, bin1, bin2, count)."""
+    lib = load_oracle()
+    band = np.ascontiguousarray(band, dtype=np.uint32)
+    offs = np.zeros(ncols + 1, dtype=np.uint64)
+    cap = int(np.count_nonzero(band))
+    b1 = np.zeros(max(cap, 1), dtype=np.int64)
+    b2 = np.zeros(max(cap, 1), dtype=np.int64)
+    cnt = np.zeros(max(cap, 1), dtype=np.uint32)
+    nnz = C.c_uint64()
+    rc = lib.orc_band_to_pixels(band.ctypes.data, nrows, ncols, bin_offset, offs.ctypes.data, b1.ctypes.data,
+                                b2.ctypes.data, cnt.ctypes.data, cap, C.byref(nnz))
+    assert rc == 0
+    n = nnz.value
+    return offs, b1[:n], b2[:n], cnt[:n]
+
+
+def random_band(rng, nrows, ncols, density=0.3):
+    """A band with zeros outside the upper triangle's reachable rows, like a simulated one."""
+    band = np.zeros((ncols, nrows), dtype=np.uint32)  # band[j, r] = column j, row r
+    vals = rng.integers(1, 1000, size=band.shape, dtype=np.uint32)
+    mask = rng.random(band.shape) < density
+    band[mask] = vals[mask]
+    band[np.arange(ncols)[:, None] < np.arange(nrows)[None, :]] = 0  # row r > column j is unused
+    return band.reshape(-1)
 
 
 def oracle_config(overrides=None, transform=False):
