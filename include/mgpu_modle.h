@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define MGPU_ABI_VERSION 1
+#define MGPU_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------------------- */
 #define MGPU_OK 0
@@ -123,6 +123,9 @@ typedef struct mgpu_config {
   uint32_t rev_speed_set;
   uint32_t fwd_speed_set;
   uint32_t occupancy_set;
+  /* optional outputs that change what a cell computes (simulation_config.hpp:86, :111) */
+  uint32_t track_1d_lef_position;    /* sample the 1D LEF occupancy after the contacts */
+  uint32_t log_model_internal_state; /* per-epoch model-state records (dump_stats) */
 } mgpu_config;
 
 /* One chromosome (the simulated range of modle::Chromosome, src/libmodle/internal/genome.cpp). */
@@ -312,6 +315,50 @@ int mgpu_simulate_cells_noalloc(mgpu_ctx* ctx, int chrom_id, const uint64_t* cel
 int mgpu_band_to_pixels(mgpu_ctx* ctx, const uint32_t* band, uint64_t nrows, uint64_t ncols,
                         uint64_t bin_offset, uint64_t* bin1_offset, int64_t* bin1, int64_t* bin2,
                         uint32_t* count, uint64_t capacity, uint64_t* nnz);
+
+/*
+ * One epoch of one cell as Simulation::dump_stats logs it (simulation.cpp:1166-1224), taken
+ * after extrude and before release_lefs when log_model_internal_state is set.  The effective
+ * barrier occupancy is barriers_occupied / nbarriers; collision counts add the rev and fwd
+ * units whose word holds that event as a collision.
+ */
+typedef struct mgpu_epoch_record {
+  uint64_t epoch;
+  uint64_t cell;              /* index of the cell in the call */
+  uint64_t burnin;            /* 1 while the burn-in is running */
+  uint64_t barriers_occupied;
+  uint64_t nbarriers;
+  uint64_t num_lefs;          /* active LEFs */
+  uint64_t stalled_rev;       /* rev units with a collision */
+  uint64_t stalled_fwd;
+  uint64_t stalled_both;      /* LEFs with both units stalled */
+  uint64_t lef_bar;           /* LEF-BAR collisions (rev + fwd) */
+  uint64_t lef_lef_primary;
+  uint64_t lef_lef_secondary;
+  double avg_loop_size;       /* stats::mean of fwd - rev over the active LEFs */
+} mgpu_epoch_record;
+
+/* Outputs beyond the band (all optional, device or host pointers). */
+typedef struct mgpu_extra_outputs {
+  /* with track_1d_lef_position: Chromosome::lef_1d_occupancy, ceil(chrom size / bin size)
+   * counters, ADDED to (register_1d_lef_occupancy, register_contacts.cpp:200-232).  When the
+   * config flag is set the sampling happens (and draws from the cell's stream) even if this
+   * pointer is NULL. */
+  uint64_t* lef_1d_occupancy;
+  /* with log_model_internal_state: records of cell i go to epoch_records[i * max_epoch_records
+   * + k] for its first max_epoch_records epochs; records_written[i] receives the number of
+   * records kept (ncells entries). */
+  mgpu_epoch_record* epoch_records;
+  uint64_t max_epoch_records;
+  uint64_t* records_written;
+} mgpu_extra_outputs;
+
+/* mgpu_simulate_cells with the optional outputs of mgpu_extra_outputs (extra may be NULL). */
+int mgpu_simulate_cells_ex(mgpu_ctx* ctx, int chrom_id, const uint64_t* cell_seeds,
+                           const uint64_t* target_contacts, uint64_t target_epochs,
+                           uint64_t num_lefs, uint64_t ncells, uint32_t* band,
+                           uint64_t* missed_updates, mgpu_cell_stats* stats,
+                           const mgpu_extra_outputs* extra);
 
 /* ---- parity and debugging entry points (used by the test-suite) ------------------------ */
 

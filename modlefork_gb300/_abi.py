@@ -64,6 +64,7 @@ class Config(C.Structure):
         ("burnin_speed_coefficient", f64), ("fwd_extrusion_speed_burnin", u64),
         ("rev_extrusion_speed_burnin", u64),
         ("rev_speed_set", u32), ("fwd_speed_set", u32), ("occupancy_set", u32),
+        ("track_1d_lef_position", u32), ("log_model_internal_state", u32),
     ]
 
     def as_dict(self):
@@ -84,6 +85,18 @@ class CellStats(C.Structure):
     _fields_ = [("epochs", u64), ("burnin_epochs", u64), ("contacts", u64),
                 ("missed_updates", u64), ("lef_epochs", u64), ("rng_draws", u64),
                 ("sort_fallbacks", u64), ("status", u64)]
+
+
+class EpochRecord(C.Structure):
+    _fields_ = [("epoch", u64), ("cell", u64), ("burnin", u64), ("barriers_occupied", u64),
+                ("nbarriers", u64), ("num_lefs", u64), ("stalled_rev", u64), ("stalled_fwd", u64),
+                ("stalled_both", u64), ("lef_bar", u64), ("lef_lef_primary", u64),
+                ("lef_lef_secondary", u64), ("avg_loop_size", C.c_double)]
+
+
+class ExtraOutputs(C.Structure):
+    _fields_ = [("lef_1d_occupancy", C.c_void_p), ("epoch_records", C.c_void_p),
+                ("max_epoch_records", u64), ("records_written", C.c_void_p)]
 
 
 class TraceHeader(C.Structure):

@@ -102,6 +102,7 @@ struct Scalars {
   u64 n5, n3;
   u32 hist_size, hist_head;
   u64 bc0, bc1, bc2;  // broadcast slots for lane 0 results
+  u64 nrec;           // model-state records written for this cell
   u64* prof;          // profile counters of the launch (device memory) or null
 };
 static_assert(sizeof(Scalars) <= CELL_HEADER_BYTES, "scalars do not fit the cell header");
@@ -2186,7 +2187,17 @@ __device__ __forceinline__ u32 contact_attempt(const Cell& c, const KParams& P, 
 }
 
 // Lane 0: one contact attempt with serial draws (the exact path for rejections).
-__device__ void contact_attempt_serial(Cell& c, const KParams& P, bool tad, u64 na, bool* ok, bool* miss) {
+// register_1d_lef_occupancy (register_contacts.cpp:200-232): one count in each of the two bins
+__device__ __forceinline__ void occ_increment(const KParams& P, u64 i1, u64 i2) {
+  if (!P.occ) return;
+  if (i1 < P.occ_bins) atomicAdd(&P.occ[i1], 1ull);
+  if (i2 < P.occ_bins) atomicAdd(&P.occ[i2], 1ull);
+}
+
+// One attempt of register_contacts_loop / _tad (register_contacts.cpp:129-198) or, with occ, of
+// register_1d_lef_occupancy (the loop attempt with the 1D counters as its sink); lane 0.
+__device__ void contact_attempt_serial(Cell& c, const KParams& P, bool tad, u64 na, bool* ok, bool* miss,
+                                       bool occ = false) {
   *ok = false;
   *miss = false;
   const u64 start = (u64)P.start + 1, end = (u64)P.end - 1;
@@ -2200,7 +2211,9 @@ __device__ void contact_attempt_serial(Cell& c, const KParams& P, bool tad, u64 
   const double b = (double)fp + n2;
   const double p1 = fmin(a, b), p2 = fmax(a, b);
   if (!(p1 >= (double)start && p2 >= (double)start && p1 < (double)end && p2 < (double)end)) return;
-  if (!tad) {
+  if (occ) {
+    occ_increment(P, ((u64)p1 - start) / P.bin, ((u64)p2 - start) / P.bin);
+  } else if (!tad) {
     *miss = band_increment(c, P, ((u64)p1 - start) / P.bin, ((u64)p2 - start) / P.bin);
   } else {
     const u64 p11 = s_uniform_int(c, (u64)p1, (u64)p2);
@@ -2244,9 +2257,10 @@ __device__ void sample_contacts(Cell& c, u64* s, const KParams& P, u64 target) {
   const bool serial = P.debug_flags & DBG_SERIAL_CONTACTS;
   u64 budget = 1000 * num + 1000000;  // attempts before giving up (see DEV_ERR_NO_BOUND_LEF)
   u32 missed = 0;
-  for (int pass = 0; pass < 2; ++pass) {
-    const bool tad = pass == 1;
-    u64 todo = tad ? num - n_loop : n_loop;
+  const int passes = P.track_occ ? 3 : 2;  // loop, TAD, then the 1D occupancy
+  for (int pass = 0; pass < passes; ++pass) {
+    const bool tad = pass == 1, occ = pass == 2;
+    u64 todo = occ ? num : (tad ? num - n_loop : n_loop);
     const u32 nominal = 1 + (P.noisify ? 2 : 0) + (tad ? 2 : 0);
     while (todo != 0) {
       if (budget < 32) {
@@ -2272,7 +2286,13 @@ __device__ void sample_contacts(Cell& c, u64* s, const KParams& P, u64 target) {
         lim = (u32)__ffs(mm);
       }
       const unsigned lanes = lim >= 32 ? FULL : ((1u << lim) - 1);
-      if (ok && ((lanes >> ln()) & 1u) && band_increment(c, P, row, col)) ++missed;
+      if (ok && ((lanes >> ln()) & 1u)) {
+        if (occ) {
+          occ_increment(P, row, col);
+        } else if (band_increment(c, P, row, col)) {
+          ++missed;
+        }
+      }
       const u32 draws = lim == 0 ? 0 : (lim - 1) * nominal + __shfl_sync(FULL, used, lim == 0 ? 0 : lim - 1);
       todo -= __popc(okm & lanes);
       __syncwarp();
@@ -2283,7 +2303,7 @@ __device__ void sample_contacts(Cell& c, u64* s, const KParams& P, u64 target) {
         prof_add(c, PF_CONTACT_SERIAL, 1);
         if (ln() == 0) {
           bool sok, smiss;
-          contact_attempt_serial(c, P, tad, na, &sok, &smiss);
+          contact_attempt_serial(c, P, tad, na, &sok, &smiss, occ);
           sc->bc1 = sok ? 1 : 0;
           if (smiss) sc->missed++;
         }
@@ -2319,15 +2339,16 @@ __device__ void sample_contacts_serial(Cell& c, const KParams& P, u64 target) {
     n_loop = (u64)s_binomial(c, P, (i64)num, P.p_loop);
   }
   u64 budget = 1000 * num + 1000000;
-  for (int pass = 0; pass < 2; ++pass) {
-    u64 todo = pass == 0 ? n_loop : num - n_loop;
+  const int passes = P.track_occ ? 3 : 2;  // loop, TAD, then the 1D occupancy
+  for (int pass = 0; pass < passes; ++pass) {
+    u64 todo = pass == 0 ? n_loop : (pass == 1 ? num - n_loop : num);
     while (todo != 0) {
       if (--budget == 0 || sc->status != DEV_OK) {
         set_status(c, DEV_ERR_NO_BOUND_LEF);
         return;
       }
       bool ok, miss;
-      contact_attempt_serial(c, P, pass == 1, sc->num_active, &ok, &miss);
+      contact_attempt_serial(c, P, pass == 1, sc->num_active, &ok, &miss, pass == 2);
       if (miss) sc->missed++;
       if (ok) --todo;
     }
@@ -2445,6 +2466,7 @@ __device__ void cell_reset(Cell& c, u32 nl, u64 seed) {
     }
     sc->rpos = 0;
     sc->gpos = 0;
+    sc->nrec = 0;
     sc->lanes_stale = 1;
     sc->status = DEV_OK;
     sc->epoch = 0;
@@ -2464,8 +2486,59 @@ __device__ void cell_reset(Cell& c, u32 nl, u64 seed) {
   __syncwarp();
 }
 
+// Simulation::dump_stats (simulation.cpp:1166-1224): the epoch's model-state record, taken after
+// extrude and before release_lefs; the loop-size mean is exact (an integer sum below 2^53).
+__device__ void log_model_state(Cell& c, const KParams& P, u32 n, u64 cell) {
+  Scalars* sc = c.sc;
+  if (!P.records || sc->nrec >= P.rec_max) return;
+  u32 st_rev = 0, st_fwd = 0, st_both = 0, lb = 0, pri = 0, sec = 0;
+  u64 loop = 0;
+  for (u32 i = ln(); i < n; i += 32) {
+    const u32 r = c.rc[i], f = c.fc[i];
+    const bool sr = cw_occurred(r), sf = cw_occurred(f);
+    st_rev += sr;
+    st_fwd += sf;
+    st_both += sr && sf;
+    lb += cw_occurred_as(r, EV_LEF_BAR) + cw_occurred_as(f, EV_LEF_BAR);
+    pri += cw_occurred_as(r, EV_PRIMARY) + cw_occurred_as(f, EV_PRIMARY);
+    sec += cw_occurred_as(r, EV_SECONDARY) + cw_occurred_as(f, EV_SECONDARY);
+    loop += pos64(c.fwd[i]) - pos64(c.rev[i]);
+  }
+  u32 occ = 0;
+  for (u32 w = ln(); w < (c.nb + 31) / 32; w += 32) occ += __popc(c.bst[w]);
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    st_rev += __shfl_xor_sync(FULL, st_rev, d);
+    st_fwd += __shfl_xor_sync(FULL, st_fwd, d);
+    st_both += __shfl_xor_sync(FULL, st_both, d);
+    lb += __shfl_xor_sync(FULL, lb, d);
+    pri += __shfl_xor_sync(FULL, pri, d);
+    sec += __shfl_xor_sync(FULL, sec, d);
+    loop += __shfl_xor_sync(FULL, loop, d);
+    occ += __shfl_xor_sync(FULL, occ, d);
+  }
+  if (ln() == 0) {
+    mgpu_epoch_record* r = P.records + cell * P.rec_max + sc->nrec;
+    r->epoch = sc->epoch;
+    r->cell = cell;
+    r->burnin = sc->burnin_completed ? 0 : 1;
+    r->barriers_occupied = occ;
+    r->nbarriers = c.nb;
+    r->num_lefs = n;
+    r->stalled_rev = st_rev;
+    r->stalled_fwd = st_fwd;
+    r->stalled_both = st_both;
+    r->lef_bar = lb;
+    r->lef_lef_primary = pri;
+    r->lef_lef_secondary = sec;
+    r->avg_loop_size = n ? (double)loop / (double)n : 0.0;
+    sc->nrec++;
+  }
+  __syncwarp();
+}
+
 __device__ void run_cell(Cell& c, u64* s, const KParams& P, const CellTask& task, u64 target_epochs,
-                         const DevTrace* trace, mgpu_cell_stats* stats) {
+                         const DevTrace* trace, mgpu_cell_stats* stats, u64 cell) {
   Scalars* sc = c.sc;
   const u32 nl = P.nlefs;
   cell_reset(c, nl, task.seed);
@@ -2533,6 +2606,7 @@ __device__ void run_cell(Cell& c, u64* s, const KParams& P, const CellTask& task
     process_collisions(c, s, P, n, true);
     ta = clock64();
     extrude(c, n);
+    if (P.log_state) log_model_state(c, P, n, cell);
     release_lefs(c, s, P, n, completed);
     tb = clock64();
     prof_add(c, PF_EXTRUDE_RELEASE, tb - ta);
@@ -2545,6 +2619,7 @@ __device__ void run_cell(Cell& c, u64* s, const KParams& P, const CellTask& task
     if (sc->status != DEV_OK) break;
   }
   if (ln() == 0) {
+    if (P.rec_count) P.rec_count[cell] = sc->nrec;
     if (trace && trace->num_recorded) *trace->num_recorded = sc->epoch;
     if (stats) {
       stats->epochs = sc->epoch;
@@ -2575,7 +2650,7 @@ __global__ void __launch_bounds__(32) simulate_kernel(const __grid_constant__ KP
     if (ln() == 0) cell = atomicAdd(work, 1u);
     cell = __shfl_sync(FULL, cell, 0);
     if (cell >= ncells) break;
-    run_cell(c, s, P, tasks[cell], target_epochs, tracing ? &trace : nullptr, stats ? stats + cell : nullptr);
+    run_cell(c, s, P, tasks[cell], target_epochs, tracing ? &trace : nullptr, stats ? stats + cell : nullptr, cell);
     if (ln() == 0 && missed) atomicAdd((unsigned long long*)missed, (unsigned long long)c.sc->missed);
     __syncwarp();
   }

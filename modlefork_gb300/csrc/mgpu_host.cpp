@@ -764,6 +764,9 @@ static int make_kparams(const mgpu_ctx* ctx, const ChromEntry& ch, uint64_t nlef
   P->pos_bucket = bucket;
   P->pos_range = range;
   P->debug_flags = ctx->debug_flags;
+  P->track_occ = c.track_1d_lef_position ? 1u : 0u;
+  P->log_state = c.log_model_internal_state ? 1u : 0u;
+  P->occ_bins = (ch.chrom.size + c.bin_size - 1) / c.bin_size;
   // Layout: the header (scalars, PRNG ring, burn-in history, barrier bits) is always on chip;
   // per-LEF arrays go on chip in priority order while they fit, the rest into a global slot.
   const u64 header = cell_header_bytes(ch.nb, P->hist_cap);
@@ -893,7 +896,8 @@ static int status_from_stats(const mgpu_cell_stats* st, uint64_t n) {
 
 static int run_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* seeds, const uint64_t* targets,
                      uint64_t target_epochs, uint64_t nlefs, uint64_t ncells, uint32_t* band,
-                     uint64_t* missed, mgpu_cell_stats* stats, const DevTrace* trace) {
+                     uint64_t* missed, mgpu_cell_stats* stats, const DevTrace* trace,
+                     const mgpu_extra_outputs* extra = nullptr) {
   if (chrom_id < 0 || chrom_id >= (int)ctx->chroms.size())
     return fail(MGPU_ERR_INVALID_ARG, "unknown chromosome handle %d", chrom_id);
   if (ncells == 0) return MGPU_OK;
@@ -933,6 +937,26 @@ static int run_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* seeds, const u
     rc = ensure_scratch(ctx, P, resident_cells(P, ncells));
     if (rc) return rc;
   }
+  // optional outputs: occupancy counters are added to; records land where the caller wants them
+  DevBuf d_occ, d_rec, d_recn;
+  if (extra && extra->lef_1d_occupancy && P.track_occ) {
+    rc = to_device(extra->lef_1d_occupancy, P.occ_bins * sizeof(uint64_t), d_occ, st, true);
+    if (rc) return rc;
+    P.occ = (unsigned long long*)d_occ.p;
+  }
+  const uint64_t rec_max = extra ? extra->max_epoch_records : 0;
+  if (extra && extra->epoch_records && rec_max && P.log_state) {
+    if (ncells > UINT64_MAX / rec_max / sizeof(mgpu_epoch_record))
+      return fail(MGPU_ERR_INVALID_ARG, "too many epoch records requested");
+    rc = to_device(extra->epoch_records, ncells * rec_max * sizeof(mgpu_epoch_record), d_rec, st, false);
+    if (rc) return rc;
+    rc = alloc_on_stream(d_recn, ncells * sizeof(uint64_t), st);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(d_recn.p, 0, ncells * sizeof(uint64_t), st));
+    P.records = (mgpu_epoch_record*)d_rec.p;
+    P.rec_max = rec_max;
+    P.rec_count = (u64*)d_recn.p;
+  }
   P.prof = ctx->d_prof;
   CK(cudaMemsetAsync(ctx->d_prof, 0, 32 * sizeof(uint64_t), st));
   CK(cudaEventRecord(ctx->ev0, st));
@@ -942,6 +966,15 @@ static int run_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* seeds, const u
   if (rc) return fail(rc, "%s", err);
   CK(cudaEventRecord(ctx->ev1, st));
   if (band && d_band.owned) CK(cudaMemcpyAsync(band, d_band.p, band_bytes, cudaMemcpyDeviceToHost, st));
+  if (P.occ && d_occ.owned)
+    CK(cudaMemcpyAsync(extra->lef_1d_occupancy, d_occ.p, P.occ_bins * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+  if (P.records) {
+    if (d_rec.owned)
+      CK(cudaMemcpyAsync(extra->epoch_records, d_rec.p, ncells * rec_max * sizeof(mgpu_epoch_record),
+                         cudaMemcpyDeviceToHost, st));
+    if (extra->records_written)
+      CK(cudaMemcpyAsync(extra->records_written, d_recn.p, ncells * sizeof(uint64_t), cudaMemcpyDefault, st));
+  }
   uint64_t h_missed = 0;
   CK(cudaMemcpyAsync(&h_missed, d_missed.p, 8, cudaMemcpyDeviceToHost, st));
   std::vector<mgpu_cell_stats> h_stats(ncells);
@@ -1112,6 +1145,18 @@ extern "C" int mgpu_simulate_cells_noalloc(mgpu_ctx* ctx, int chrom_id, const ui
                        sizeof(err));
   if (rc) return fail(rc, "%s", err);
   return MGPU_OK;
+}
+
+extern "C" int mgpu_simulate_cells_ex(mgpu_ctx* ctx, int chrom_id, const uint64_t* cell_seeds,
+                                      const uint64_t* target_contacts, uint64_t target_epochs,
+                                      uint64_t num_lefs, uint64_t ncells, uint32_t* band,
+                                      uint64_t* missed_updates, mgpu_cell_stats* stats,
+                                      const mgpu_extra_outputs* extra) {
+  if (!ctx) return fail(MGPU_ERR_INVALID_ARG, "mgpu_simulate_cells_ex: null context");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  CK(cudaSetDevice(ctx->device));
+  return run_cells(ctx, chrom_id, cell_seeds, target_contacts, target_epochs, num_lefs, ncells,
+                   band, missed_updates, stats, nullptr, extra);
 }
 
 extern "C" int mgpu_trace_cell(mgpu_ctx* ctx, int chrom_id, uint64_t cell_seed,

@@ -108,6 +108,14 @@ struct KParams {
   u64 slot_bytes;  // global scratch of one resident cell (arrays that do not fit on chip)
   u32 debug_flags; // DBG_* bits: force the exact serial implementation of a step
   u64* prof;       // per-launch profile counters (32 entries, device memory) or null
+  // optional outputs (mgpu_extra_outputs)
+  u32 track_occ;               // sample the 1D LEF occupancy (draws even without a buffer)
+  u32 log_state;               // write per-epoch model-state records
+  unsigned long long* occ;     // occupancy counters (occ_bins entries) or null
+  u64 occ_bins;
+  mgpu_epoch_record* records;  // records of cell i at records + i * rec_max, or null
+  u64 rec_max;
+  u64* rec_count;              // per cell number of records written, or null
 };
 
 // Per-LEF arrays of a cell, in on-chip placement priority order.  SR and SF are adjacent:

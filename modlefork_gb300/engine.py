@@ -59,6 +59,8 @@ def load(path=LIB_PATH):
                                       C.c_void_p, C.c_void_p, C.c_void_p]),
         "mgpu_simulate_cells_noalloc": (i32, [C.c_void_p, i32, C.c_void_p, C.c_void_p, u64, u64, u64,
                                               C.c_void_p, C.c_void_p, C.c_void_p]),
+        "mgpu_simulate_cells_ex": (i32, [C.c_void_p, i32, C.c_void_p, C.c_void_p, u64, u64, u64,
+                                         C.c_void_p, C.c_void_p, C.c_void_p, P(abi.ExtraOutputs)]),
         "mgpu_band_to_pixels": (i32, [C.c_void_p, C.c_void_p, u64, u64, u64, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.c_void_p, u64, P(u64)]),
         "mgpu_trace_cell": (i32, [C.c_void_p, i32, u64, u64, u64, u64, C.c_void_p,
@@ -245,6 +247,36 @@ class Engine:
                                             C.addressof(missed), C.addressof(st) if st else None),
                "mgpu_simulate_cells")
         return missed.value, st
+
+    def simulate_cells_ex(self, chrom_id, seeds, targets, target_epochs, nlefs, band, occupancy=None,
+                          max_epoch_records=0):
+        """mgpu_simulate_cells_ex with host arrays: ``occupancy`` (uint64, ceil(size / bin)
+        counters) is added to when the config tracks the 1D LEF occupancy; with
+        ``max_epoch_records`` and log_model_internal_state the per-epoch model-state records are
+        returned.  Returns (missed, stats, records) where records[i] lists cell i's records."""
+        seeds = np.ascontiguousarray(seeds, dtype=np.uint64)
+        targets = np.ascontiguousarray(targets, dtype=np.uint64)
+        n = len(seeds)
+        missed = C.c_uint64(0)
+        st = (abi.CellStats * n)()
+        ex = abi.ExtraOutputs()
+        if occupancy is not None:
+            assert occupancy.dtype == np.uint64 and occupancy.flags["C_CONTIGUOUS"]
+            ex.lef_1d_occupancy = occupancy.ctypes.data
+        recs = written = None
+        if max_epoch_records:
+            recs = (abi.EpochRecord * (n * max_epoch_records))()
+            written = np.zeros(n, dtype=np.uint64)
+            ex.epoch_records = C.addressof(recs)
+            ex.max_epoch_records = max_epoch_records
+            ex.records_written = written.ctypes.data
+        _check(self.lib.mgpu_simulate_cells_ex(self.h, chrom_id, seeds.ctypes.data, targets.ctypes.data,
+                                               target_epochs, nlefs, n, band.ctypes.data, C.addressof(missed),
+                                               C.addressof(st), C.byref(ex)), "mgpu_simulate_cells_ex")
+        out = None
+        if recs is not None:
+            out = [[recs[i * max_epoch_records + k] for k in range(int(written[i]))] for i in range(n)]
+        return missed.value, st, out
 
     def band_to_pixels(self, band, nrows, ncols, bin_offset=0):
         """mgpu_band_to_pixels on a host uint32 band: returns (bin1_offset, bin1, bin2, count)

@@ -1458,7 +1458,51 @@ class Cell {
         --todo;
       }
     }
+    // register_1d_lef_occupancy (register_contacts.cpp:200-232): the loop attempt again, with
+    // one count in each of the two bins of Chromosome::lef_1d_occupancy as its sink
+    if (c.track_1d_lef_position) {
+      todo = num_events;
+      while (todo != 0) {
+        const Lef& l = lefs[uniform_int(g, 0, num_active - 1)];
+        if (l.bound() && within(l)) {
+          const auto [p1, p2] = noise_pair(l);
+          if (!pos_ok(p1, p2)) continue;
+          const bp_t i1 = (static_cast<bp_t>(p1) - start) / c.bin_size;
+          const bp_t i2 = (static_cast<bp_t>(p2) - start) / c.bin_size;
+          if (occ) {
+            occ[i1]++;
+            occ[i2]++;
+          }
+          --todo;
+        }
+      }
+    }
     num_contacts += num_events;
+  }
+
+  // Simulation::dump_stats (simulation.cpp:1166-1224) as a record
+  void dump_stats() {
+    if (!recs || nrec >= rec_max) return;
+    mgpu_epoch_record r{};
+    r.epoch = epoch;
+    r.cell = cell_index;
+    r.burnin = burnin_completed ? 0 : 1;
+    for (usize i = 0; i < b.size(); ++i) r.barriers_occupied += b.is_active(i) ? 1 : 0;
+    r.nbarriers = b.size();
+    r.num_lefs = num_active;
+    double acc = 0.0;
+    for (usize i = 0; i < num_active; ++i) {
+      const bool sr = rc[i].occurred(), sf = fc[i].occurred();
+      r.stalled_rev += sr;
+      r.stalled_fwd += sf;
+      r.stalled_both += sr && sf;
+      r.lef_bar += rc[i].occurred(LEF_BAR) + fc[i].occurred(LEF_BAR);
+      r.lef_lef_primary += rc[i].occurred(LEF_LEF_PRIMARY) + fc[i].occurred(LEF_LEF_PRIMARY);
+      r.lef_lef_secondary += rc[i].occurred(LEF_LEF_SECONDARY) + fc[i].occurred(LEF_LEF_SECONDARY);
+      acc = acc + static_cast<double>(lefs[i].fwd - lefs[i].rev);
+    }
+    r.avg_loop_size = num_active ? acc / static_cast<double>(num_active) : 0.0;
+    recs[nrec++] = r;
   }
 
   void record(mgpu_trace_request* tr, u64 rec_idx, usize n5, usize n3) {
@@ -1495,6 +1539,11 @@ class Cell {
       }
     }
   }
+
+  // optional outputs: 1D occupancy counters and model-state records
+  u64* occ = nullptr;
+  mgpu_epoch_record* recs = nullptr;
+  u64 rec_max = 0, nrec = 0, cell_index = 0;
 
   CellResult run(u64 seed, u64 target_contacts, u64 target_epochs, Band& band,
                  mgpu_trace_request* tr) {
@@ -1535,6 +1584,7 @@ class Cell {
       const auto [n5, n3] =
           sim.process_collisions(ch, lefs, n, b, rr, fr, rm, fm, rc, fc, g, true, &ub);
       Sim::extrude(lefs, n, rm, fm);
+      if (c.log_model_internal_state) dump_stats();
       sim.release_lefs(lefs, n, b, rc, fc, g, burnin_completed);
       if (tr) record(tr, rec, n5, n3);
       ++rec;
@@ -1764,10 +1814,29 @@ uint64_t orc_sample(uint64_t seed, int kind, uint64_t a, uint64_t b, double p, d
   return g.ndraws;
 }
 
+int orc_simulate_cell_ex(const mgpu_config* cfg, const mgpu_chrom* chrom, const mgpu_barrier* bs,
+                         uint64_t nb, uint64_t seed, uint64_t target_contacts,
+                         uint64_t target_epochs, uint64_t nlefs, uint32_t* band,
+                         mgpu_cell_stats* stats, mgpu_trace_request* trace, uint64_t* occupancy,
+                         mgpu_epoch_record* records, uint64_t max_records, uint64_t cell_index,
+                         uint64_t* records_written);
+
 int orc_simulate_cell(const mgpu_config* cfg, const mgpu_chrom* chrom, const mgpu_barrier* bs,
                       uint64_t nb, uint64_t seed, uint64_t target_contacts,
                       uint64_t target_epochs, uint64_t nlefs, uint32_t* band,
                       mgpu_cell_stats* stats, mgpu_trace_request* trace) {
+  return orc_simulate_cell_ex(cfg, chrom, bs, nb, seed, target_contacts, target_epochs, nlefs, band,
+                              stats, trace, nullptr, nullptr, 0, 0, nullptr);
+}
+
+// orc_simulate_cell with the optional outputs: occupancy has ceil(chrom size / bin) counters
+// (added to), records receives the cell's first max_records model-state records.
+int orc_simulate_cell_ex(const mgpu_config* cfg, const mgpu_chrom* chrom, const mgpu_barrier* bs,
+                         uint64_t nb, uint64_t seed, uint64_t target_contacts,
+                         uint64_t target_epochs, uint64_t nlefs, uint32_t* band,
+                         mgpu_cell_stats* stats, mgpu_trace_request* trace, uint64_t* occupancy,
+                         mgpu_epoch_record* records, uint64_t max_records, uint64_t cell_index,
+                         uint64_t* records_written) {
   if (!cfg || !chrom || nlefs == 0) return MGPU_ERR_INVALID_ARG;
   const Chrom ch{chrom->start, chrom->end};
   Barriers b = make_barriers(bs, nb);
@@ -1777,7 +1846,12 @@ int orc_simulate_cell(const mgpu_config* cfg, const mgpu_chrom* chrom, const mgp
   bd.ncols = (ch.end - ch.start + cfg->bin_size - 1) / cfg->bin_size;
   bd.data = band;
   Cell cell(*cfg, ch, b, nlefs);
+  cell.occ = occupancy;
+  cell.recs = records;
+  cell.rec_max = max_records;
+  cell.cell_index = cell_index;
   const CellResult r = cell.run(seed, target_contacts, target_epochs, bd, trace);
+  if (records_written) *records_written = cell.nrec;
   if (stats) {
     stats->epochs = r.epochs;
     stats->burnin_epochs = r.burnin_epochs;

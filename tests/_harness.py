@@ -60,6 +60,11 @@ def load_oracle():
     lib.orc_run_phase.argtypes = [P(abi.Config), P(abi.Chrom), P(abi.Barrier), C.c_uint64,
                                   C.c_int, P(abi.PhaseIO)]
     lib.orc_run_phase.restype = C.c_int
+    lib.orc_simulate_cell_ex.argtypes = [P(abi.Config), P(abi.Chrom), P(abi.Barrier), C.c_uint64,
+                                         C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64,
+                                         P(C.c_uint32), P(abi.CellStats), P(abi.TraceRequest),
+                                         C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64, P(C.c_uint64)]
+    lib.orc_simulate_cell_ex.restype = C.c_int
     lib.orc_band_to_pixels.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, P(C.c_uint64)]
     lib.orc_band_to_pixels.restype = C.c_int

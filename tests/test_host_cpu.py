@@ -24,6 +24,7 @@ def lib():
 
 def header_functions():
     text = open(os.path.join(ROOT, "include", "mgpu_modle.h")).read()
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)  # declarations only, not comments
     return sorted(set(re.findall(r"\b(mgpu_[a-z0-9_]+)\s*\(", text)))
 
 
@@ -39,7 +40,9 @@ def test_struct_layouts_match_header(lib):
     assert C.sizeof(abi.Barrier) == 32
     assert C.sizeof(abi.CellStats) == 64
     assert C.sizeof(abi.TraceHeader) == 72
-    assert lib.mgpu_abi_version() == 1
+    assert C.sizeof(abi.EpochRecord) == 104
+    assert C.sizeof(abi.ExtraOutputs) == 32
+    assert lib.mgpu_abi_version() == 2
 
 
 OVERRIDES = [
