@@ -14,12 +14,14 @@ from . import engine
 
 
 class ChromResult:
-    def __init__(self, chrom, nlefs, band, missed, stats):
+    def __init__(self, chrom, nlefs, band, missed, stats, occupancy=None, records=None):
         self.chrom = chrom
         self.nlefs = nlefs
         self.band = band
         self.missed = missed
         self.stats = stats
+        self.occupancy = occupancy  # 1D LEF occupancy counters (track_1d_lef_position)
+        self.records = records      # per-cell lists of model-state records (log_model_internal_state)
 
     @property
     def lef_epochs(self):
@@ -49,7 +51,7 @@ CONCURRENT_SMEM_BUDGET = 32 * 1024
 
 
 def simulate_genome(cfg, genome, ncells=None, device=0, simulate_wo_barriers=False, workers=1,
-                    smem_budget=None):
+                    smem_budget=None, max_epoch_records=4096):
     """Run every cell of every chromosome; returns a list of ChromResult in genome order.
 
     With ``workers`` > 1, that many host threads each drive their own engine context (own
@@ -80,9 +82,17 @@ def simulate_genome(cfg, genome, ncells=None, device=0, simulate_wo_barriers=Fal
                         return
                     t = prepare_chrom(eng, cfg, chrom, barriers, ncells)
                     band = np.zeros(t["nrows"] * t["ncols"], dtype=np.uint32)
-                    missed, stats = eng.simulate_cells(t["cid"], t["seeds"], t["targets"],
-                                                       t["target_epochs"], t["nlefs"], band)
-                    results[i] = ChromResult(chrom, t["nlefs"], band, missed, stats)
+                    occ, recs = None, None
+                    if cfg.track_1d_lef_position or cfg.log_model_internal_state:
+                        if cfg.track_1d_lef_position:
+                            occ = np.zeros((chrom.size + cfg.bin_size - 1) // cfg.bin_size, dtype=np.uint64)
+                        missed, stats, recs = eng.simulate_cells_ex(
+                            t["cid"], t["seeds"], t["targets"], t["target_epochs"], t["nlefs"], band,
+                            occupancy=occ, max_epoch_records=max_epoch_records if cfg.log_model_internal_state else 0)
+                    else:
+                        missed, stats = eng.simulate_cells(t["cid"], t["seeds"], t["targets"],
+                                                           t["target_epochs"], t["nlefs"], band)
+                    results[i] = ChromResult(chrom, t["nlefs"], band, missed, stats, occ, recs)
         except BaseException as e:  # surfaced to the caller below
             errors.append(e)
 
@@ -94,6 +104,43 @@ def simulate_genome(cfg, genome, ncells=None, device=0, simulate_wo_barriers=Fal
     if errors:
         raise errors[0]
     return [results[i] for i, _, _ in jobs]
+
+def write_lef_occupancy(path, cfg, results):
+    """The 1D LEF occupancy track as bedGraph (chrom, start, end, value), with the values the
+    reference writes to its bigwig (Simulation::write_1d_lef_occupancy_to_disk,
+    simulation.cpp:214-262): each chromosome's counters divided by its maximum, as float32, one
+    interval per bin from the chromosome's start."""
+    bin_size = int(cfg.bin_size)
+    with open(path, "w") as f:
+        for r in results:
+            if r.occupancy is None:
+                continue
+            mx = int(r.occupancy.max()) if r.occupancy.size else 0
+            vals = (r.occupancy.astype(np.float64) / float(mx)).astype(np.float32) if mx else \
+                np.zeros(r.occupancy.size, np.float32)
+            for k, v in enumerate(vals.tolist()):
+                s0 = r.chrom.start + k * bin_size
+                f.write(f"{r.chrom.name}\t{s0}\t{min(s0 + bin_size, r.chrom.size)}\t{v!r}\n")
+
+
+def write_model_state(path, results):
+    """Model-state log with the columns of Simulation::dump_stats (simulation.cpp:1166-1224):
+    task, epoch, cell, chrom, burn-in, effective barrier occupancy, LEFs, stalled rev / fwd /
+    both, LEF-BAR, primary and secondary LEF-LEF collisions, mean loop size.  The task id is the
+    chromosome's index in the run times the cell count plus the cell."""
+    with open(path, "w") as f:
+        for ci, r in enumerate(results):
+            if r.records is None:
+                continue
+            ncells = len(r.records)
+            for cell, recs in enumerate(r.records):
+                for x in recs:
+                    occ = x.barriers_occupied / x.nbarriers if x.nbarriers else float("nan")
+                    f.write("\t".join(str(v) for v in (
+                        ci * ncells + cell, x.epoch, cell, r.chrom.name, "True" if x.burnin else "False", occ,
+                        x.num_lefs, x.stalled_rev, x.stalled_fwd, x.stalled_both, x.lef_bar,
+                        x.lef_lef_primary, x.lef_lef_secondary, x.avg_loop_size)) + "\n")
+
 
 def genome_pixels(cfg, results, genome_chroms=None):
     """Genome-wide pixel table of a run, as a cooler stores it (Cooler::write_or_append_cmatrix_to_file,
@@ -141,12 +188,16 @@ def _main(argv=None):
     ap.add_argument("--workers", type=int, default=1, help="concurrent chromosome launches")
     ap.add_argument("--smem-budget", type=int, default=None, help="shared memory per cell (bytes)")
     ap.add_argument("--pixels", default=None, help="write the pixel table (bin1_id, bin2_id, count) as TSV")
+    ap.add_argument("--lef-occupancy", default=None, help="track the 1D LEF occupancy, write it as bedGraph")
+    ap.add_argument("--model-state", default=None, help="log the per-epoch model state as TSV")
     args = ap.parse_args(argv)
     cfg, g = gen.parity_10mbp() if args.workload == "parity" else gen.genome_24chr()
     if args.chrom:
         g = [g[i] for i in args.chrom]
     if args.cells is not None:
         cfg.num_cells = args.cells
+    cfg.track_1d_lef_position = 1 if args.lef_occupancy else 0
+    cfg.log_model_internal_state = 1 if args.model_state else 0
     t0 = time.perf_counter()
     res = simulate_genome(cfg, g, device=args.device, workers=args.workers, smem_budget=args.smem_budget)
     dt = time.perf_counter() - t0
@@ -156,6 +207,10 @@ def _main(argv=None):
             f.write("bin1_id\tbin2_id\tcount\n")
             for a, b, c in zip(b1.tolist(), b2.tolist(), cnt.tolist()):
                 f.write(f"{a}\t{b}\t{c}\n")
+    if args.lef_occupancy:
+        write_lef_occupancy(args.lef_occupancy, cfg, res)
+    if args.model_state:
+        write_model_state(args.model_state, res)
     le = sum(r.lef_epochs for r in res)
     print(json.dumps({"workload": args.workload, "chromosomes": [r.chrom.name for r in res],
                       "cells": int(cfg.num_cells), "workers": args.workers, "lef_epochs": le, "contacts": sum(r.contacts for r in res),
