@@ -360,6 +360,30 @@ int mgpu_simulate_cells_ex(mgpu_ctx* ctx, int chrom_id, const uint64_t* cell_see
                            uint64_t* missed_updates, mgpu_cell_stats* stats,
                            const mgpu_extra_outputs* extra);
 
+/*
+ * Batched launch (no counterpart in the reference, whose worker threads pop one (chromosome,
+ * cell) task at a time, scheduler_simulate.cpp:229-256): the cells of many chromosomes or
+ * windows advance in one persistent kernel with a work queue, largest first.  Task i is one
+ * simulate_one_cell call on chromosome handle chrom_id with its own seed, targets and LEF
+ * count.  bands[chrom_id] (nbands entries, host or device pointers, NULL where no task uses the
+ * chromosome) receives the contacts, added to; missed[chrom_id] is incremented (may be NULL);
+ * stats[i] is task i's outcome (may be NULL).  Results equal one mgpu_simulate_cells call per
+ * chromosome.  A shared-memory budget set with mgpu_set_debug_flags applies to every cell;
+ * without one, large batches use 32 KiB per cell so that many cells share an SM.
+ */
+typedef struct mgpu_batch_task {
+  uint64_t seed;
+  uint64_t target_contacts;
+  uint64_t target_epochs;
+  uint64_t num_lefs;
+  int32_t chrom_id;
+  uint32_t reserved;
+} mgpu_batch_task;
+
+int mgpu_simulate_batch(mgpu_ctx* ctx, const mgpu_batch_task* tasks, uint64_t ntasks,
+                        uint32_t* const* bands, uint64_t nbands, uint64_t* missed,
+                        mgpu_cell_stats* stats);
+
 /* ---- parity and debugging entry points (used by the test-suite) ------------------------ */
 
 /*

@@ -94,6 +94,11 @@ class EpochRecord(C.Structure):
                 ("lef_lef_secondary", u64), ("avg_loop_size", C.c_double)]
 
 
+class BatchTask(C.Structure):
+    _fields_ = [("seed", u64), ("target_contacts", u64), ("target_epochs", u64), ("num_lefs", u64),
+                ("chrom_id", C.c_int32), ("reserved", u32)]
+
+
 class ExtraOutputs(C.Structure):
     _fields_ = [("lef_1d_occupancy", C.c_void_p), ("epoch_records", C.c_void_p),
                 ("max_epoch_records", u64), ("records_written", C.c_void_p)]

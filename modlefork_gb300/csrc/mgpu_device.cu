@@ -2656,6 +2656,41 @@ __global__ void __launch_bounds__(32) simulate_kernel(const __grid_constant__ KP
   }
 }
 
+// Batched persistent kernel: cells of many chromosomes or windows in one work queue.  Each
+// task names its plan (parameters, layout, barrier track, band); a warp copies the plan's
+// parameters into shared memory when its next cell belongs to another plan than the last.
+__global__ void __launch_bounds__(32) simulate_batch_kernel(const BatchPlan* plans, const BatchTask* tasks,
+                                                            u64 ntasks, u64 slot_bytes,
+                                                            mgpu_cell_stats* stats, const ulonglong2* jt,
+                                                            u32* work, char* gscratch) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ Cell c;
+  __shared__ __align__(16) KParams Psh;
+  u64 s[4] = {0, 0, 0, 0};
+  char* gslot = gscratch + (u64)blockIdx.x * slot_bytes;
+  u32 cur = 0xFFFFFFFFu;
+  for (;;) {
+    u32 cell = 0;
+    if (ln() == 0) cell = atomicAdd(work, 1u);
+    cell = __shfl_sync(FULL, cell, 0);
+    if (cell >= ntasks) break;
+    const BatchTask t = tasks[cell];
+    const BatchPlan& pl = plans[t.plan];
+    if (t.plan != cur) {
+      const u32* src = reinterpret_cast<const u32*>(&pl.P);
+      u32* dst = reinterpret_cast<u32*>(&Psh);
+      for (u32 w = ln(); w < sizeof(KParams) / 4; w += 32) dst[w] = src[w];
+      __syncwarp();
+      carve(c, smem, gslot, Psh, Psh.nlefs, pl.ch, jt, pl.band);
+      cur = t.plan;
+    }
+    const CellTask ct{t.seed, t.target_contacts};
+    run_cell(c, s, Psh, ct, pl.target_epochs, nullptr, stats ? stats + cell : nullptr, cell);
+    if (ln() == 0 && pl.missed) atomicAdd(pl.missed, (unsigned long long)c.sc->missed);
+    __syncwarp();
+  }
+}
+
 // One step of the epoch loop on caller state (mgpu_run_phase).
 __global__ void __launch_bounds__(32) phase_kernel(const __grid_constant__ KParams P, DevChrom ch, int phase,
                                                    u32 n, u64* arrays, u64* bind_mask,
@@ -2849,6 +2884,8 @@ u64 max_smem_per_block() {
   cudaFuncAttributes a{};
   if (cudaFuncGetAttributes(&a, simulate_kernel) == cudaSuccess) stat = a.sharedSizeBytes;
   if (cudaFuncGetAttributes(&a, phase_kernel) == cudaSuccess && a.sharedSizeBytes > stat) stat = a.sharedSizeBytes;
+  if (cudaFuncGetAttributes(&a, simulate_batch_kernel) == cudaSuccess && a.sharedSizeBytes > stat)
+    stat = a.sharedSizeBytes;
   cudaGetLastError();
   return (u64)v > stat ? (u64)v - stat : 0;
 }
@@ -2903,6 +2940,44 @@ int launch_simulate(const KParams& P, const DevChrom& ch, const CellTask* tasks,
                                                              (const ulonglong2*)jump_table, work_counter,
                                                              gscratch);
   return cuda_fail(cudaGetLastError(), "simulate_kernel launch", errbuf, errlen);
+}
+
+u64 resident_batch_cells(u32 smem_bytes, u64 ntasks) {
+  if (cudaFuncSetAttribute(simulate_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)max_smem_per_block()) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, simulate_batch_kernel, 32, smem_bytes) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const u64 grid = (u64)sms * (u64)(per_sm > 0 ? per_sm : 1);
+  return grid < ntasks ? grid : ntasks;
+}
+
+int launch_simulate_batch(const BatchPlan* plans, const BatchTask* tasks, u64 ntasks, u32 smem_bytes,
+                          u64 slot_bytes, mgpu_cell_stats* stats, const void* jump_table, u32* work_counter,
+                          char* gscratch, u64 gscratch_bytes, void* stream, char* errbuf, int errlen) {
+  u64 grid = resident_batch_cells(smem_bytes, ntasks);
+  if (grid == 0) return ntasks ? MGPU_ERR_CUDA : MGPU_OK;
+  if (slot_bytes && gscratch_bytes / slot_bytes < grid) grid = gscratch_bytes / slot_bytes;
+  if (grid == 0) {
+    if (errbuf) snprintf(errbuf, errlen, "global scratch too small for one cell");
+    return MGPU_ERR_INTERNAL;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = cuda_fail(cudaMemsetAsync(work_counter, 0, sizeof(u32), st), "memset", errbuf, errlen);
+  if (rc) return rc;
+  simulate_batch_kernel<<<(unsigned)grid, 32, smem_bytes, st>>>(plans, tasks, ntasks, slot_bytes, stats,
+                                                                 (const ulonglong2*)jump_table, work_counter,
+                                                                 gscratch);
+  return cuda_fail(cudaGetLastError(), "simulate_batch_kernel launch", errbuf, errlen);
 }
 
 int launch_phase(const KParams& P, const DevChrom& ch, int phase, u64 n, u64* arrays,

@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -691,7 +692,8 @@ extern "C" int mgpu_upload_chrom(mgpu_ctx* ctx, const mgpu_chrom* chrom, const m
   return MGPU_OK;
 }
 
-static int make_kparams(const mgpu_ctx* ctx, const ChromEntry& ch, uint64_t nlefs, KParams* P) {
+static int make_kparams(const mgpu_ctx* ctx, const ChromEntry& ch, uint64_t nlefs, KParams* P,
+                        uint64_t budget_override = 0) {
   const mgpu_config& c = ctx->cfg;
   std::memset(P, 0, sizeof(*P));
   if (nlefs == 0) return fail(MGPU_ERR_INVALID_ARG, "num_lefs must be positive");
@@ -770,7 +772,8 @@ static int make_kparams(const mgpu_ctx* ctx, const ChromEntry& ch, uint64_t nlef
   // Layout: the header (scalars, PRNG ring, burn-in history, barrier bits) is always on chip;
   // per-LEF arrays go on chip in priority order while they fit, the rest into a global slot.
   const u64 header = cell_header_bytes(ch.nb, P->hist_cap);
-  const u64 limit = std::min<u64>(ctx->smem_limit, ctx->smem_budget ? ctx->smem_budget : ctx->smem_limit);
+  const u64 budget = budget_override ? budget_override : ctx->smem_budget;
+  const u64 limit = std::min<u64>(ctx->smem_limit, budget ? budget : ctx->smem_limit);
   if (header > limit)
     return fail(MGPU_ERR_UNSUPPORTED, "%u barriers need %llu B of shared memory (limit %llu)", ch.nb,
                 (unsigned long long)header, (unsigned long long)limit);
@@ -1018,6 +1021,152 @@ extern "C" int mgpu_simulate_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* 
   CK(cudaSetDevice(ctx->device));
   return run_cells(ctx, chrom_id, cell_seeds, target_contacts, target_epochs, num_lefs, ncells,
                    band, missed_updates, stats, nullptr);
+}
+
+extern "C" int mgpu_simulate_batch(mgpu_ctx* ctx, const mgpu_batch_task* tasks, uint64_t ntasks,
+                                   uint32_t* const* bands, uint64_t nbands, uint64_t* missed,
+                                   mgpu_cell_stats* stats) {
+  if (!ctx || (ntasks && !tasks)) return fail(MGPU_ERR_INVALID_ARG, "mgpu_simulate_batch: null argument");
+  if (ntasks == 0) return MGPU_OK;
+  if (ntasks >= 0xFFFFFFFFull) return fail(MGPU_ERR_INVALID_ARG, "mgpu_simulate_batch: too many tasks");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t st = active_stream(ctx);
+  // plans: one per (chromosome, LEF count, target epochs)
+  struct Key {
+    int chrom;
+    uint64_t nlefs, te;
+    bool operator<(const Key& o) const {
+      return chrom != o.chrom ? chrom < o.chrom : (nlefs != o.nlefs ? nlefs < o.nlefs : te < o.te);
+    }
+  };
+  std::map<Key, u32> plan_of;
+  std::vector<Key> keys;
+  for (uint64_t i = 0; i < ntasks; ++i) {
+    const mgpu_batch_task& t = tasks[i];
+    if (t.chrom_id < 0 || t.chrom_id >= (int)ctx->chroms.size())
+      return fail(MGPU_ERR_INVALID_ARG, "task %llu: unknown chromosome handle %d", (unsigned long long)i, t.chrom_id);
+    if ((uint64_t)t.chrom_id >= nbands || !bands || !bands[t.chrom_id])
+      return fail(MGPU_ERR_INVALID_ARG, "task %llu: no band for chromosome handle %d", (unsigned long long)i,
+                  t.chrom_id);
+    const Key k{t.chrom_id, t.num_lefs, t.target_epochs};
+    if (!plan_of.count(k)) {
+      plan_of[k] = (u32)keys.size();
+      keys.push_back(k);
+    }
+  }
+  int dev_sms = 0;
+  cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  const uint64_t budget = ctx->smem_budget ? ctx->smem_budget
+                                           : (ntasks >= 8ull * (uint64_t)dev_sms ? 32768ull : 0ull);
+  std::vector<BatchPlan> plans(keys.size());
+  u32 smem_bytes = 0;
+  u64 slot_bytes = 0;
+  for (size_t p = 0; p < keys.size(); ++p) {
+    const ChromEntry& ch = ctx->chroms[keys[p].chrom];
+    int rc = make_kparams(ctx, ch, keys[p].nlefs, &plans[p].P, budget);
+    if (rc) return rc;
+    plans[p].ch = DevChrom{ch.d_bars, ch.d_pos_flags, ch.nb};
+    plans[p].target_epochs = keys[p].te;
+    smem_bytes = std::max(smem_bytes, plans[p].P.smem_bytes);
+    slot_bytes = std::max<u64>(slot_bytes, plans[p].P.slot_bytes);
+  }
+  // bands of the chromosomes in use
+  std::map<int, DevBuf> dband;
+  for (const Key& k : keys) {
+    if (dband.count(k.chrom)) continue;
+    const KParams& P0 = plans[plan_of[k]].P;
+    const size_t bytes = (size_t)P0.nrows * P0.ncols * sizeof(uint32_t);
+    int rc = to_device(bands[k.chrom], bytes, dband[k.chrom], st, true);
+    if (rc) return rc;
+  }
+  DevBuf d_missed;
+  int rc = alloc_on_stream(d_missed, keys.size() * sizeof(uint64_t), st);
+  if (rc) return rc;
+  CK(cudaMemsetAsync(d_missed.p, 0, keys.size() * sizeof(uint64_t), st));
+  for (size_t p = 0; p < keys.size(); ++p) {
+    plans[p].band = (u32*)dband[keys[p].chrom].p;
+    plans[p].missed = (unsigned long long*)d_missed.p + p;
+    plans[p].P.prof = nullptr;
+  }
+  // work queue: largest LEF count first, cells of one plan together
+  std::vector<uint64_t> order(ntasks);
+  for (uint64_t i = 0; i < ntasks; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) {
+    const uint64_t na = tasks[a].num_lefs, nb = tasks[b].num_lefs;
+    if (na != nb) return na > nb;
+    return plan_of[Key{tasks[a].chrom_id, tasks[a].num_lefs, tasks[a].target_epochs}] <
+           plan_of[Key{tasks[b].chrom_id, tasks[b].num_lefs, tasks[b].target_epochs}];
+  });
+  std::vector<BatchTask> bt(ntasks);
+  for (uint64_t k = 0; k < ntasks; ++k) {
+    const mgpu_batch_task& t = tasks[order[k]];
+    bt[k] = BatchTask{t.seed, t.target_contacts, plan_of[Key{t.chrom_id, t.num_lefs, t.target_epochs}], 0};
+  }
+  DevBuf d_plans, d_tasks, d_stats;
+  rc = alloc_on_stream(d_plans, plans.size() * sizeof(BatchPlan), st);
+  if (!rc) rc = alloc_on_stream(d_tasks, ntasks * sizeof(BatchTask), st);
+  if (!rc) rc = alloc_on_stream(d_stats, ntasks * sizeof(mgpu_cell_stats), st);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(d_plans.p, plans.data(), plans.size() * sizeof(BatchPlan), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d_tasks.p, bt.data(), ntasks * sizeof(BatchTask), cudaMemcpyHostToDevice, st));
+  if (slot_bytes) {
+    KParams Pslot = plans[0].P;
+    Pslot.slot_bytes = slot_bytes;
+    rc = ensure_scratch(ctx, Pslot, resident_batch_cells(smem_bytes, ntasks));
+    if (rc) return rc;
+  }
+  char err[256] = {0};
+  CK(cudaEventRecord(ctx->ev0, st));
+  rc = launch_simulate_batch((const BatchPlan*)d_plans.p, (const BatchTask*)d_tasks.p, ntasks, smem_bytes,
+                             slot_bytes, (mgpu_cell_stats*)d_stats.p, ctx->d_jump, ctx->d_work, ctx->d_scratch,
+                             ctx->scratch_bytes, st, err, sizeof(err));
+  if (rc) return fail(rc, "%s", err);
+  CK(cudaEventRecord(ctx->ev1, st));
+  for (auto& kv : dband) {
+    if (kv.second.owned) {
+      const KParams* P0 = nullptr;
+      for (size_t p = 0; p < keys.size(); ++p)
+        if (keys[p].chrom == kv.first) P0 = &plans[p].P;
+      CK(cudaMemcpyAsync(bands[kv.first], kv.second.p, (size_t)P0->nrows * P0->ncols * sizeof(uint32_t),
+                         cudaMemcpyDeviceToHost, st));
+    }
+  }
+  std::vector<uint64_t> h_missed(keys.size());
+  std::vector<mgpu_cell_stats> h_stats(ntasks);
+  CK(cudaMemcpyAsync(h_missed.data(), d_missed.p, keys.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(h_stats.data(), d_stats.p, ntasks * sizeof(mgpu_cell_stats), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    ctx->last_kernel_ms = ms;
+  }
+  if (missed) {
+    std::vector<uint64_t> add(nbands, 0);
+    for (size_t p = 0; p < keys.size(); ++p) add[keys[p].chrom] += h_missed[p];
+    if (is_device_ptr(missed)) {
+      std::vector<uint64_t> cur(nbands);
+      CK(cudaMemcpyAsync(cur.data(), missed, nbands * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      for (uint64_t c = 0; c < nbands; ++c) cur[c] += add[c];
+      CK(cudaMemcpyAsync(missed, cur.data(), nbands * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
+    } else {
+      for (uint64_t c = 0; c < nbands; ++c) missed[c] += add[c];
+    }
+  }
+  std::vector<mgpu_cell_stats> out(ntasks);
+  for (uint64_t k = 0; k < ntasks; ++k) out[order[k]] = h_stats[k];
+  if (stats) {
+    if (is_device_ptr(stats)) {
+      CK(cudaMemcpyAsync(stats, out.data(), ntasks * sizeof(mgpu_cell_stats), cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
+    } else {
+      std::memcpy(stats, out.data(), ntasks * sizeof(mgpu_cell_stats));
+    }
+  }
+  return status_from_stats(out.data(), ntasks);
 }
 
 // Copy a device result to the caller's buffer (host or device).

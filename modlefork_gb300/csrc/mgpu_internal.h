@@ -191,6 +191,26 @@ constexpr u64 NOALLOC_TASKS_OFFSET = 256;
 constexpr u64 NOALLOC_SLOTS_OFFSET =
     (NOALLOC_TASKS_OFFSET + (u64)MGPU_NOALLOC_MAX_CELLS * sizeof(CellTask) + 255) & ~255ull;
 static_assert(NOALLOC_SLOTS_OFFSET < MGPU_NOALLOC_SCRATCH_BYTES, "task list larger than the scratch");
+// Batched launch: many (chromosome or window, LEF count) plans, one work queue of cells.
+struct BatchPlan {
+  KParams P;  // layout planned under the launch's common shared-memory size
+  DevChrom ch;
+  u32* band;
+  unsigned long long* missed;  // this plan's missed updates (device)
+  u64 target_epochs;
+};
+struct BatchTask {
+  u64 seed;
+  u64 target_contacts;
+  u32 plan;
+  u32 pad;
+};
+int launch_simulate_batch(const BatchPlan* plans, const BatchTask* tasks, u64 ntasks, u32 smem_bytes,
+                          u64 slot_bytes, mgpu_cell_stats* stats, const void* jump_table, u32* work_counter,
+                          char* gscratch, u64 gscratch_bytes, void* stream, char* errbuf, int errlen);
+// Grid of a batched launch with the given per-cell shared memory.
+u64 resident_batch_cells(u32 smem_bytes, u64 ntasks);
+
 // Pixel table of a band (mgpu_pixels.cu): counts[i] = non-zero pixels of bin1 row i,
 // offsets[0..ncols] their exclusive scan; then the (bin1, bin2, count) pixels.
 int launch_band_counts(const u32* band, u64 nrows, u64 ncols, u32* counts, u64* offsets, void* stream,

@@ -61,6 +61,8 @@ def load(path=LIB_PATH):
                                               C.c_void_p, C.c_void_p, C.c_void_p]),
         "mgpu_simulate_cells_ex": (i32, [C.c_void_p, i32, C.c_void_p, C.c_void_p, u64, u64, u64,
                                          C.c_void_p, C.c_void_p, C.c_void_p, P(abi.ExtraOutputs)]),
+        "mgpu_simulate_batch": (i32, [C.c_void_p, P(abi.BatchTask), u64, P(C.c_void_p), u64, C.c_void_p,
+                                      C.c_void_p]),
         "mgpu_band_to_pixels": (i32, [C.c_void_p, C.c_void_p, u64, u64, u64, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.c_void_p, u64, P(u64)]),
         "mgpu_trace_cell": (i32, [C.c_void_p, i32, u64, u64, u64, u64, C.c_void_p,
@@ -277,6 +279,32 @@ class Engine:
         if recs is not None:
             out = [[recs[i * max_epoch_records + k] for k in range(int(written[i]))] for i in range(n)]
         return missed.value, st, out
+
+    def simulate_batch(self, tasks, bands):
+        """mgpu_simulate_batch.  ``tasks`` is a sequence of (chrom_id, seed, target_contacts,
+        target_epochs, num_lefs); ``bands`` maps chrom_id to a host uint32 array or a device
+        pointer.  Returns (missed per chrom_id, per-task stats)."""
+        n = len(tasks)
+        arr = (abi.BatchTask * n)()
+        for i, (cid, seed, tc, te, nl) in enumerate(tasks):
+            arr[i].chrom_id = cid
+            arr[i].seed = int(seed)
+            arr[i].target_contacts = int(tc)
+            arr[i].target_epochs = int(te)
+            arr[i].num_lefs = int(nl)
+        nb = max(bands) + 1 if bands else 0
+        ptrs = (C.c_void_p * max(nb, 1))()
+        for cid, b in bands.items():
+            if isinstance(b, np.ndarray):
+                assert b.dtype == np.uint32 and b.flags["C_CONTIGUOUS"]
+                ptrs[cid] = b.ctypes.data
+            else:
+                ptrs[cid] = b
+        missed = np.zeros(max(nb, 1), dtype=np.uint64)
+        st = (abi.CellStats * n)()
+        _check(self.lib.mgpu_simulate_batch(self.h, arr, n, ptrs, nb, missed.ctypes.data, C.addressof(st)),
+               "mgpu_simulate_batch")
+        return {cid: int(missed[cid]) for cid in bands}, st
 
     def band_to_pixels(self, band, nrows, ncols, bin_offset=0):
         """mgpu_band_to_pixels on a host uint32 band: returns (bin1_offset, bin1, bin2, count)

@@ -105,6 +105,29 @@ def simulate_genome(cfg, genome, ncells=None, device=0, simulate_wo_barriers=Fal
         raise errors[0]
     return [results[i] for i, _, _ in jobs]
 
+def simulate_genome_batched(cfg, genome, ncells=None, device=0, simulate_wo_barriers=False):
+    """simulate_genome with every chromosome's cells in one batched launch (mgpu_simulate_batch):
+    one persistent kernel and one work queue for the whole genome, largest chromosomes first.
+    Same results as one launch per chromosome."""
+    ncells = int(cfg.num_cells if ncells is None else ncells)
+    jobs = [(c, b) for c, b in genome if b or simulate_wo_barriers]
+    with engine.Engine(cfg, device) as eng:
+        preps, tasks, bands = [], [], {}
+        for chrom, barriers in jobs:
+            t = prepare_chrom(eng, cfg, chrom, barriers, ncells)
+            preps.append(t)
+            bands[t["cid"]] = np.zeros(t["nrows"] * t["ncols"], dtype=np.uint32)
+            for seed, target in zip(t["seeds"], t["targets"]):
+                tasks.append((t["cid"], int(seed), int(target), t["target_epochs"], t["nlefs"]))
+        missed, stats = eng.simulate_batch(tasks, bands)
+    out, k = [], 0
+    for t in preps:
+        st = stats[k:k + ncells]
+        k += ncells
+        out.append(ChromResult(t["chrom"], t["nlefs"], bands[t["cid"]], missed[t["cid"]], st))
+    return out
+
+
 def write_lef_occupancy(path, cfg, results):
     """The 1D LEF occupancy track as bedGraph (chrom, start, end, value), with the values the
     reference writes to its bigwig (Simulation::write_1d_lef_occupancy_to_disk,
@@ -186,6 +209,7 @@ def _main(argv=None):
     ap.add_argument("--cells", type=int, default=None)
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--workers", type=int, default=1, help="concurrent chromosome launches")
+    ap.add_argument("--batched", action="store_true", help="all chromosomes in one batched launch")
     ap.add_argument("--smem-budget", type=int, default=None, help="shared memory per cell (bytes)")
     ap.add_argument("--pixels", default=None, help="write the pixel table (bin1_id, bin2_id, count) as TSV")
     ap.add_argument("--lef-occupancy", default=None, help="track the 1D LEF occupancy, write it as bedGraph")
@@ -199,7 +223,10 @@ def _main(argv=None):
     cfg.track_1d_lef_position = 1 if args.lef_occupancy else 0
     cfg.log_model_internal_state = 1 if args.model_state else 0
     t0 = time.perf_counter()
-    res = simulate_genome(cfg, g, device=args.device, workers=args.workers, smem_budget=args.smem_budget)
+    if args.batched:
+        res = simulate_genome_batched(cfg, g, device=args.device)
+    else:
+        res = simulate_genome(cfg, g, device=args.device, workers=args.workers, smem_budget=args.smem_budget)
     dt = time.perf_counter() - t0
     if args.pixels:
         b1, b2, cnt = genome_pixels(cfg, res, [c for c, _ in g])

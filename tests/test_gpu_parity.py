@@ -277,3 +277,42 @@ def test_unreachable_contacts_end_with_timeout_status():
         with pytest.raises(engine.EngineError) as e:
             eng.simulate_cells(cid, np.array([1], dtype=np.uint64), np.array([10], dtype=np.uint64), 0, 4, band)
     assert e.value.code == abi.MGPU_ERR_TIMEOUT
+
+
+@pytest.mark.parametrize("mode", list(MODES))
+def test_batched_launch_matches_per_chromosome_launches(mode):
+    """One batched launch over several chromosomes (and two LEF counts on one of them) gives
+    the bands, missed updates and per-cell results of one launch per (chromosome, LEF count)."""
+    cfg, gen = genome.genome_24chr(seed=5, nchroms=3, min_len=2_000_000, max_len=6_000_000)
+    n = 12
+    with engine.Engine(cfg) as eng:
+        eng.set_debug_flags(*MODES[mode])
+        tasks, bands, want = [], {}, []
+        for chrom, bars in gen:
+            cid = eng.upload_chrom(chrom, bars)
+            nl = engine.num_lefs(cfg, chrom.simulated_size)
+            nrows, ncols = engine.band_shape(cfg, chrom.simulated_size)
+            for nl_k in ((nl, nl + 7) if cid == 1 else (nl,)):
+                targets, te = engine.task_targets(cfg, chrom.simulated_size, nl_k, n)
+                seeds = np.array([engine.cell_seed(chrom.name, chrom.size, cfg.seed, i) for i in range(n)],
+                                 dtype=np.uint64) + nl_k
+                band = np.zeros(nrows * ncols, dtype=np.uint32)
+                m, st = eng.simulate_cells(cid, seeds, targets, te, nl_k, band)
+                want.append((cid, band, m, [(s.epochs, s.contacts, s.rng_draws) for s in st]))
+                bands.setdefault(cid, np.zeros(nrows * ncols, dtype=np.uint32))
+                tasks += [(cid, int(sd), int(tg), te, nl_k) for sd, tg in zip(seeds, targets)]
+        perm = np.random.default_rng(1).permutation(len(tasks))  # task order does not matter
+        missed, st = eng.simulate_batch([tasks[i] for i in perm], bands)
+    got = {}
+    for j, i in enumerate(perm):
+        got[i] = (st[j].epochs, st[j].contacts, st[j].rng_draws)
+    k = 0
+    sums, msums = {}, {}
+    for cid, band, m, stats in want:
+        assert [got[k + t] for t in range(n)] == stats
+        k += n
+        sums[cid] = sums.get(cid, 0) + band.astype(np.uint64)
+        msums[cid] = msums.get(cid, 0) + m
+    for cid in bands:
+        assert np.array_equal(bands[cid].astype(np.uint64), sums[cid])
+        assert missed[cid] == msums[cid]
