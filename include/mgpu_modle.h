@@ -248,6 +248,15 @@ int mgpu_last_profile(mgpu_ctx* ctx, uint64_t counters[32]);
 int mgpu_upload_chrom(mgpu_ctx* ctx, const mgpu_chrom* chrom, const mgpu_barrier* barriers,
                       uint64_t nbarriers, int* chrom_id);
 
+/* A window of a chromosome for modle perturbate (Simulation::simulate_window,
+ * scheduler_perturbate.cpp:429-480): cells bind LEFs and sample contacts inside
+ * [window_start, window_end), their band covers the window (band shape of its length), while
+ * moves are still clamped by the chromosome's own range [start, end); pass the window's
+ * barriers (map_barriers_to_window, deleted ones with stp_active 0 and stp_inactive 1). */
+int mgpu_upload_window(mgpu_ctx* ctx, const mgpu_chrom* chrom, uint64_t window_start,
+                       uint64_t window_end, const mgpu_barrier* barriers, uint64_t nbarriers,
+                       int* chrom_id);
+
 /*
  * Simulate `ncells` cells of one chromosome: the drop-in for calling
  * Simulation::simulate_one_cell once per task (scheduler_simulate.cpp:229-256).

@@ -994,7 +994,7 @@ __device__ void bind_lefs(Cell& c, u64* s, const KParams& P, u32 n, u32 epoch, i
     const unsigned bad = __ballot_sync(FULL, need && !ok);
     const u32 f = bad ? (u32)(__ffs(bad) - 1) : 32u;
     if (need && ln() < f) {
-      const u32 pos = (u32)(P.start + r);
+      const u32 pos = (u32)(P.wstart + r);
       c.rev[i] = pos;
       c.fwd[i] = pos;
       c.bep[i] = epoch;
@@ -1005,7 +1005,7 @@ __device__ void bind_lefs(Cell& c, u64* s, const KParams& P, u32 n, u32 epoch, i
       if (f < 32) {  // finish this chunk serially from the rejecting LEF
         for (u32 k = i0 + f; k < min(i0 + 32, n); ++k) {
           if (!bind_selected(c, k, mode, mask)) continue;
-          const u64 pos = s_uniform_int(c, P.start, (u64)P.end - 1);
+          const u64 pos = s_uniform_int(c, P.wstart, (u64)P.wend - 1);
           c.rev[k] = (u32)pos;
           c.fwd[k] = (u32)pos;
           c.bep[k] = epoch;
@@ -2129,7 +2129,7 @@ __device__ __forceinline__ u32 contact_attempt(const Cell& c, const KParams& P, 
                                                u64* row, u64* col) {
   *ok = false;
   *regular = true;
-  const u64 start = (u64)P.start + 1, end = (u64)P.end - 1;
+  const u64 start = (u64)P.wstart + 1, end = (u64)P.wend - 1;
   u32 used = 0;
   const u64 li = ring_at(c, c.sc->rpos + off + used++) / lbucket;
   if (li > na - 1) {
@@ -2200,7 +2200,7 @@ __device__ void contact_attempt_serial(Cell& c, const KParams& P, bool tad, u64 
                                        bool occ = false) {
   *ok = false;
   *miss = false;
-  const u64 start = (u64)P.start + 1, end = (u64)P.end - 1;
+  const u64 start = (u64)P.wstart + 1, end = (u64)P.wend - 1;
   const u64 li = s_uniform_int(c, 0, na - 1);
   if (c.bep[li] == UNBOUND) return;
   const u64 rp = pos64(c.rev[li]), fp = pos64(c.fwd[li]);

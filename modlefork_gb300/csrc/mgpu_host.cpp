@@ -537,6 +537,7 @@ extern "C" uint64_t mgpu_state_digest(uint64_t n, const uint64_t* rev, const uin
 // ===========================================================================================
 struct ChromEntry {
   mgpu_chrom chrom{};
+  uint64_t ws = 0, we = 0;  // simulated window (the whole range unless uploaded as a window)
   std::string name;
   DevBarrier* d_bars = nullptr;
   uint2* d_pos_flags = nullptr;  // inside the d_bars allocation
@@ -676,6 +677,8 @@ extern "C" int mgpu_upload_chrom(mgpu_ctx* ctx, const mgpu_chrom* chrom, const m
   ChromEntry e;
   e.name.assign(chrom->name ? chrom->name : "", chrom->name ? chrom->name_len : 0);
   e.chrom = *chrom;
+  e.ws = chrom->start;
+  e.we = chrom->end;
   e.nb = (u32)nb;
   if (nb) {
     // one allocation: the DevBarrier records, then the compact {pos, flags} pairs
@@ -692,6 +695,23 @@ extern "C" int mgpu_upload_chrom(mgpu_ctx* ctx, const mgpu_chrom* chrom, const m
   return MGPU_OK;
 }
 
+extern "C" int mgpu_upload_window(mgpu_ctx* ctx, const mgpu_chrom* chrom, uint64_t window_start,
+                                  uint64_t window_end, const mgpu_barrier* barriers, uint64_t nb,
+                                  int* chrom_id) {
+  if (!ctx || !chrom || !chrom_id) return fail(MGPU_ERR_INVALID_ARG, "mgpu_upload_window: null argument");
+  if (window_start < chrom->start || window_end > chrom->end || window_end <= window_start ||
+      window_end - window_start < 3)
+    return fail(MGPU_ERR_INVALID_ARG, "window [%llu, %llu) must span at least 3 bp inside [%llu, %llu)",
+                (unsigned long long)window_start, (unsigned long long)window_end,
+                (unsigned long long)chrom->start, (unsigned long long)chrom->end);
+  const int rc = mgpu_upload_chrom(ctx, chrom, barriers, nb, chrom_id);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->chroms[*chrom_id].ws = window_start;
+  ctx->chroms[*chrom_id].we = window_end;
+  return MGPU_OK;
+}
+
 static int make_kparams(const mgpu_ctx* ctx, const ChromEntry& ch, uint64_t nlefs, KParams* P,
                         uint64_t budget_override = 0) {
   const mgpu_config& c = ctx->cfg;
@@ -700,7 +720,9 @@ static int make_kparams(const mgpu_ctx* ctx, const ChromEntry& ch, uint64_t nlef
   if (nlefs >= (1ull << 27)) return fail(MGPU_ERR_UNSUPPORTED, "too many LEFs");
   P->start = (u32)ch.chrom.start;
   P->end = (u32)ch.chrom.end;
-  const uint64_t len = ch.chrom.end - ch.chrom.start;
+  P->wstart = (u32)ch.ws;
+  P->wend = (u32)ch.we;
+  const uint64_t len = ch.we - ch.ws;
   uint64_t nrows, ncols;
   mgpu_band_shape(&c, len, &nrows, &ncols);
   P->bin = (u32)c.bin_size;
@@ -760,7 +782,7 @@ static int make_kparams(const mgpu_ctx* ctx, const ChromEntry& ch, uint64_t nlef
     const double p = (0.5 < P->p_loop) ? (1 - P->p_loop) : P->p_loop;
     P->bin_q_n = std::pow((1 - p), (double)(int64_t)P->spe);
   }
-  const uint64_t range = (uint64_t)P->end - 1 - P->start;
+  const uint64_t range = (uint64_t)P->wend - 1 - P->wstart;  // bind positions: uniform_int[ws, we - 1]
   uint64_t bucket = UINT64_MAX / (range + 1);
   if (UINT64_MAX % (range + 1) == range) ++bucket;
   P->pos_bucket = bucket;

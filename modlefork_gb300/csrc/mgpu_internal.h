@@ -71,7 +71,8 @@ struct Trial {
 };
 
 struct KParams {
-  u32 start, end;  // simulated range [start, end)
+  u32 start, end;    // chromosome range [start, end): move clamps, boundary collisions
+  u32 wstart, wend;  // simulated window: binding, contacts and the band (= start, end for a chromosome)
   u32 bin, nrows, ncols;
   u32 nlefs, nbarriers;
   u32 hist_cap, smooth_w;

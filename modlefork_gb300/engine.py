@@ -55,6 +55,7 @@ def load(path=LIB_PATH):
         "mgpu_destroy": (i32, [C.c_void_p]),
         "mgpu_sync": (i32, [C.c_void_p]),
         "mgpu_upload_chrom": (i32, [C.c_void_p, P(abi.Chrom), P(abi.Barrier), u64, P(i32)]),
+        "mgpu_upload_window": (i32, [C.c_void_p, P(abi.Chrom), u64, u64, P(abi.Barrier), u64, P(i32)]),
         "mgpu_simulate_cells": (i32, [C.c_void_p, i32, C.c_void_p, C.c_void_p, u64, u64, u64,
                                       C.c_void_p, C.c_void_p, C.c_void_p]),
         "mgpu_simulate_cells_noalloc": (i32, [C.c_void_p, i32, C.c_void_p, C.c_void_p, u64, u64, u64,
@@ -210,6 +211,17 @@ class Engine:
         cid = C.c_int()
         _check(self.lib.mgpu_upload_chrom(self.h, C.byref(ch), bs, len(barriers), C.byref(cid)),
                "mgpu_upload_chrom")
+        self.chroms[cid.value] = chrom
+        return cid.value
+
+    def upload_window(self, chrom, window_start, window_end, barriers):
+        """mgpu_upload_window: a window of ``chrom`` (binding, contacts and band inside
+        [window_start, window_end), moves clamped by the chromosome); returns the handle."""
+        ch = chrom.as_abi()
+        bs = abi.make_barriers(barriers)
+        cid = C.c_int()
+        _check(self.lib.mgpu_upload_window(self.h, C.byref(ch), window_start, window_end, bs, len(barriers),
+                                           C.byref(cid)), "mgpu_upload_window")
         self.chroms[cid.value] = chrom
         return cid.value
 

@@ -775,8 +775,13 @@ struct Band {
   }
 };
 
+// Chromosome range (move clamps, boundary collisions) and the simulated window (binding,
+// contacts, band): the window is the whole range for modle simulate and a part of it for the
+// windows of modle perturbate (Simulation::select_and_bind_lefs and
+// sample_and_register_contacts, simulation.cpp:1154-1164, register_contacts.cpp:107-108).
 struct Chrom {
   bp_t start, end;
+  bp_t ws, we;
 };
 
 // Post-transform Config fields read by the epoch loop.
@@ -1414,8 +1419,8 @@ class Cell {
   void sample_contacts(usize num_events, Band& band, u64 target) {
     if (c.target_contact_density > 0.0) num_events = std::min(num_events, target - num_contacts);
     if (num_events == 0) return;
-    const bp_t start = ch.start + 1;
-    const bp_t end = ch.end - 1;
+    const bp_t start = ch.ws + 1;
+    const bp_t end = ch.we - 1;
     const usize n_loop = num_contacts_loop(num_events, c.tad_to_loop_contact_ratio, g);
     const usize n_tad = num_events - n_loop;
     const bool noisify = (c.contact_sampling_strategy & MGPU_CS_NOISIFY) != 0;
@@ -1570,7 +1575,7 @@ class Cell {
       res.lef_epochs += num_active;
       const usize n = num_active;
       for (usize i = 0; i < n; ++i) idx[i] = lefs[i].bound() ? 0 : 1;
-      sim.bind_lefs(ch.start, ch.end, lefs, n, rr, fr, idx.data(), g, epoch);
+      sim.bind_lefs(ch.ws, ch.we, lefs, n, rr, fr, idx.data(), g, epoch);
       if (burnin_completed) {
         sample_contacts(spe, band, target_contacts);
         if (target_contacts != 0 && num_contacts >= target_contacts) break;
@@ -1632,6 +1637,12 @@ static Barriers make_barriers(const mgpu_barrier* bs, u64 nb) {
 // C API used by the Python test-suite (ctypes)
 // =========================================================================================
 using namespace orc;
+
+static int simulate_cell_on(const mgpu_config* cfg, const Chrom& ch, const mgpu_barrier* bs, uint64_t nb,
+                            uint64_t seed, uint64_t target_contacts, uint64_t target_epochs, uint64_t nlefs,
+                            uint32_t* band, mgpu_cell_stats* stats, mgpu_trace_request* trace,
+                            uint64_t* occupancy, mgpu_epoch_record* records, uint64_t max_records,
+                            uint64_t cell_index, uint64_t* records_written);
 
 extern "C" {
 
@@ -1838,12 +1849,36 @@ int orc_simulate_cell_ex(const mgpu_config* cfg, const mgpu_chrom* chrom, const 
                          mgpu_epoch_record* records, uint64_t max_records, uint64_t cell_index,
                          uint64_t* records_written) {
   if (!cfg || !chrom || nlefs == 0) return MGPU_ERR_INVALID_ARG;
-  const Chrom ch{chrom->start, chrom->end};
+  const Chrom ch{chrom->start, chrom->end, chrom->start, chrom->end};
+  return simulate_cell_on(cfg, ch, bs, nb, seed, target_contacts, target_epochs, nlefs, band, stats, trace,
+                          occupancy, records, max_records, cell_index, records_written);
+}
+
+// One cell of a modle perturbate window (Simulation::simulate_window,
+// scheduler_perturbate.cpp:429-480): LEFs bind and contacts are sampled in [ws, we), the band
+// covers the window, and moves are clamped by the chromosome's own range.
+int orc_simulate_window_cell(const mgpu_config* cfg, const mgpu_chrom* chrom, uint64_t ws, uint64_t we,
+                             const mgpu_barrier* bs, uint64_t nb, uint64_t seed, uint64_t target_contacts,
+                             uint64_t target_epochs, uint64_t nlefs, uint32_t* band, mgpu_cell_stats* stats) {
+  if (!cfg || !chrom || nlefs == 0 || ws < chrom->start || we > chrom->end || we <= ws)
+    return MGPU_ERR_INVALID_ARG;
+  const Chrom ch{chrom->start, chrom->end, ws, we};
+  return simulate_cell_on(cfg, ch, bs, nb, seed, target_contacts, target_epochs, nlefs, band, stats, nullptr,
+                          nullptr, nullptr, 0, 0, nullptr);
+}
+
+}  // extern "C"
+
+static int simulate_cell_on(const mgpu_config* cfg, const Chrom& ch, const mgpu_barrier* bs, uint64_t nb,
+                            uint64_t seed, uint64_t target_contacts, uint64_t target_epochs, uint64_t nlefs,
+                            uint32_t* band, mgpu_cell_stats* stats, mgpu_trace_request* trace,
+                            uint64_t* occupancy, mgpu_epoch_record* records, uint64_t max_records,
+                            uint64_t cell_index, uint64_t* records_written) {
   Barriers b = make_barriers(bs, nb);
   Band bd;
   bd.nrows = std::min((cfg->diagonal_width + cfg->bin_size - 1) / cfg->bin_size,
-                      (ch.end - ch.start + cfg->bin_size - 1) / cfg->bin_size);
-  bd.ncols = (ch.end - ch.start + cfg->bin_size - 1) / cfg->bin_size;
+                      (ch.we - ch.ws + cfg->bin_size - 1) / cfg->bin_size);
+  bd.ncols = (ch.we - ch.ws + cfg->bin_size - 1) / cfg->bin_size;
   bd.data = band;
   Cell cell(*cfg, ch, b, nlefs);
   cell.occ = occupancy;
@@ -1865,6 +1900,8 @@ int orc_simulate_cell_ex(const mgpu_config* cfg, const mgpu_chrom* chrom, const 
   return r.status;
 }
 
+extern "C" {
+
 // Multi-threaded driver: one worker per thread, each simulating whole cells, like the
 // reference's simulate_worker pool (scheduler_simulate.cpp:96-101, 186-284).  Contacts go to
 // one shared band with atomic increments.  Returns the wall time in seconds via *seconds.
@@ -1874,7 +1911,7 @@ int orc_simulate_cells_mt(const mgpu_config* cfg, const mgpu_chrom* chrom, const
                           uint64_t nthreads, uint32_t* band, uint64_t* missed,
                           mgpu_cell_stats* stats) {
   if (!cfg || !chrom || nlefs == 0) return MGPU_ERR_INVALID_ARG;
-  const Chrom ch{chrom->start, chrom->end};
+  const Chrom ch{chrom->start, chrom->end, chrom->start, chrom->end};
   const Barriers b = make_barriers(bs, nb);
   const u64 nrows = std::min((cfg->diagonal_width + cfg->bin_size - 1) / cfg->bin_size,
                              (ch.end - ch.start + cfg->bin_size - 1) / cfg->bin_size);
@@ -1932,7 +1969,7 @@ int orc_run_phase(const mgpu_config* cfg, const mgpu_chrom* chrom, const mgpu_ba
                   uint64_t nb, int phase, mgpu_phase_io* io) {
   if (!cfg || !chrom || !io) return MGPU_ERR_INVALID_ARG;
   const usize n = io->num_lefs;
-  const Chrom ch{chrom->start, chrom->end};
+  const Chrom ch{chrom->start, chrom->end, chrom->start, chrom->end};
   Barriers b;
   for (u64 i = 0; i < nb; ++i) {
     b.pos.push_back(bs[i].pos);

@@ -65,6 +65,10 @@ def load_oracle():
                                          P(C.c_uint32), P(abi.CellStats), P(abi.TraceRequest),
                                          C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64, P(C.c_uint64)]
     lib.orc_simulate_cell_ex.restype = C.c_int
+    lib.orc_simulate_window_cell.argtypes = [P(abi.Config), P(abi.Chrom), C.c_uint64, C.c_uint64,
+                                             P(abi.Barrier), C.c_uint64, C.c_uint64, C.c_uint64,
+                                             C.c_uint64, C.c_uint64, P(C.c_uint32), P(abi.CellStats)]
+    lib.orc_simulate_window_cell.restype = C.c_int
     lib.orc_band_to_pixels.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, P(C.c_uint64)]
     lib.orc_band_to_pixels.restype = C.c_int

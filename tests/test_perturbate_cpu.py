@@ -1,0 +1,77 @@
+"""Window and deletion generation of modle perturbate (scheduler_perturbate.cpp:186-372,
+scheduler_common.cpp:51-127), restated in modlefork_gb300.perturbate."""
+
+import numpy as np
+
+from modlefork_gb300 import engine, genome, perturbate
+
+
+def test_generate_deletions_end_one_bp_after_each_barrier():
+    bars = [dict(pos=p, stp_active=0.7, stp_inactive=0.7, blocking_dir=1) for p in (100, 0, 5)]
+    assert perturbate.generate_deletions(bars, 10) == [(0, 1), (0, 6), (91, 101)]
+
+
+def test_windows_advance_by_the_diagonal_width():
+    chrom = engine.Chromosome("chrW", 10_000)
+    w = list(perturbate.windows(chrom, 1_000))
+    assert w[0] == (0, 4000, 0, 3000)
+    assert w[1] == (0, 4000, 1000, 3000)
+    assert w[2] == (1000, 5000, 2000, 4000)
+    assert w[-1] == (8000, 10_000, 9000, 10_000)
+    assert [a for _, _, a, _ in w] == list(range(0, 10_000, 1000))
+
+
+def test_window_tasks():
+    cfg = genome.parity_config(diagonal_width=500_000)
+    rng = np.random.default_rng(3)
+    chrom = engine.Chromosome("chrW", 3_000_000)
+    bars = engine.barriers_from_bed(chrom, genome.bed_records(rng, chrom.size, 60), 0.7, 0.7)
+    dels = perturbate.generate_deletions(bars, 20_000)
+    tasks = perturbate.window_tasks(cfg, chrom, bars, dels)
+    assert [t["cell_id"] for t in tasks] == list(range(len(tasks)))
+    for t in tasks:
+        ws, we = t["window"]
+        db, de = t["deletion"]
+        assert db < we and ws < de  # the deletion overlaps the outer window
+        assert all(ws <= b["pos"] < we for b in t["barriers"])
+        off = [b for b in t["barriers"] if db <= b["pos"] < de]
+        assert all(b["stp_active"] == 0.0 and b["stp_inactive"] == 1.0 for b in off)
+        assert t["active_barriers"] == len(t["barriers"]) - len(off)
+        assert t["nlefs"] == round((we - ws) / 1e6 * cfg.number_of_lefs_per_mbp)
+        npix = ((we - ws + cfg.bin_size - 1) // cfg.bin_size) * ((cfg.diagonal_width + cfg.bin_size - 1) // cfg.bin_size)
+        assert t["target_contacts"] == max(1, round(cfg.target_contact_density * npix))
+    # every deletion overlapping a window is simulated once per window
+    n = sum(sum(1 for d in dels if d[0] < we and ws < d[1])
+            for ws, we, _, _ in perturbate.windows(chrom, cfg.diagonal_width)
+            if any(ws <= b["pos"] < we for b in bars))
+    assert len(tasks) == n
+
+
+def test_oracle_window_spanning_the_chromosome_is_the_plain_cell():
+    import ctypes as C
+
+    from _harness import load_oracle, make_chrom
+    from modlefork_gb300 import _abi as abi
+
+    cfg, gen = genome.parity_10mbp(seed=9)
+    chrom, bars = gen[0]
+    nl = engine.num_lefs(cfg, chrom.simulated_size)
+    targets, te = engine.task_targets(cfg, chrom.simulated_size, nl, 64)
+    lib = load_oracle()
+    nrows, ncols = engine.band_shape(cfg, chrom.simulated_size)
+    bs = abi.make_barriers(bars)
+    ch = make_chrom(0, chrom.end, chrom.size, b"chrS")
+    out = []
+    for window in (False, True):
+        band = np.zeros(nrows * ncols, dtype=np.uint32)
+        st = abi.CellStats()
+        if window:
+            rc = lib.orc_simulate_window_cell(C.byref(cfg), C.byref(ch), 0, chrom.end, bs, len(bars), 11,
+                                              int(targets[0]), te, nl, band.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                              C.byref(st))
+        else:
+            rc = lib.orc_simulate_cell(C.byref(cfg), C.byref(ch), bs, len(bars), 11, int(targets[0]), te, nl,
+                                       band.ctypes.data_as(C.POINTER(C.c_uint32)), C.byref(st), None)
+        assert rc == 0
+        out.append((band, (st.epochs, st.contacts, st.rng_draws)))
+    assert np.array_equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
