@@ -51,6 +51,7 @@ def parse_args():
     ap.add_argument("--workers", type=int, default=12, help="concurrent engine contexts")
     ap.add_argument("--wave", type=int, default=12, help="chromosome launches per step")
     ap.add_argument("--smem-budget", type=int, default=None, help="shared memory per cell (bytes)")
+    ap.add_argument("--batched", type=int, default=1, help="also time the one-launch batched engine")
     return ap.parse_args()
 
 
@@ -349,16 +350,12 @@ def run_ours(args):
     agg = tally(done)
     log(f"timed region: {ms:.1f} ms")
     if world > 1:
-        import torch.distributed as dist
+        from modlefork_gb300 import sharding
 
-        tm = torch.tensor([ms], device=dev)
-        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
-        ms = float(tm.item())
-        for k in ("lef_epochs", "cells", "contacts", "bytes", "launches"):
-            v = torch.tensor([agg[k]], dtype=torch.float64, device=dev)
-            dist.all_reduce(v)
-            agg[k] = v.item()
-        dist.barrier()
+        ms, sums = sharding.reduce_timing(ms, {k: agg[k] for k in ("lef_epochs", "cells", "contacts", "bytes",
+                                                                    "launches")}, device=dev)
+        agg.update(sums)
+        torch.distributed.barrier()
 
     # end to end through the C ABI with host buffers (copies inside the timed region)
     e2e = None
@@ -379,6 +376,38 @@ def run_ours(args):
         e2e = {"value": eagg["lef_epochs"] / dt, "unit": "LEF-epochs/s",
                "h2d_bytes_per_step": h2d // args.e2e_steps, "d2h_bytes_per_step": d2h // args.e2e_steps,
                "steps": args.e2e_steps, "cells_per_s": eagg["cells"] / dt}
+
+    # batched: the whole genome in one launch and work queue (mgpu_simulate_batch)
+    batched = None
+    if args.batched:
+        w0 = workers[0]
+        w0["eng"].set_debug_flags(0, 0)
+        btasks = [(w0["cids"][k], int(sd), int(tg), t["te"], t["nlefs"])
+                  for k, t in enumerate(tasks) for sd, tg in zip(t["seeds"], t["targets"])]
+        dbands = {w0["cids"][k]: t["d_band"].data_ptr() for k, t in enumerate(tasks)}
+        log("batched warm-up")
+        w0["eng"].simulate_batch([x for x in btasks if x[0] in set(list(dbands)[:4])],
+                                 {c: dbands[c] for c in list(dbands)[:4]})
+        torch.cuda.synchronize()
+        log("batched timed launch")
+        bev0, bev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        bev0.record(w0["stream"])
+        _, bst = w0["eng"].simulate_batch(btasks, dbands)
+        bev1.record(w0["stream"])
+        torch.cuda.synchronize()
+        bms = bev0.elapsed_time(bev1)
+        ble = sum(x.lef_epochs for x in bst)
+        hb = {w0["cids"][k]: np.zeros(t["nrows"] * t["ncols"], dtype=np.uint32) for k, t in enumerate(tasks)}
+        log("batched end to end")
+        t0 = time.perf_counter()
+        _, bst2 = w0["eng"].simulate_batch(btasks, hb)
+        bdt = time.perf_counter() - t0
+        batched = {"value": ble / (bms / 1e3), "unit": "LEF-epochs/s", "ms": bms, "launches": 1,
+                   "cells_per_s": len(bst) / (bms / 1e3),
+                   "config": "the same 24 chromosomes x 512 cells in one batched launch, 32 KiB per cell",
+                   "e2e": {"value": sum(x.lef_epochs for x in bst2) / bdt, "unit": "LEF-epochs/s",
+                           "h2d_bytes_per_step": int(sum(b.nbytes for b in hb.values()) + len(btasks) * 40),
+                           "d2h_bytes_per_step": int(sum(b.nbytes for b in hb.values()) + len(btasks) * 64)}}
 
     if rank != 0:
         return
@@ -409,7 +438,7 @@ def run_ours(args):
                      "peak_source": f"{peak_kind} hbm_gbs", "kernel": "simulate_kernel",
                      "bytes_model": "24*LEF_epochs + 6*barriers*epochs + 8*contacts, summed over the "
                                     "launches of the timed region / region time (launches overlap)"},
-        "e2e": e2e, "clocks": clk,
+        "e2e": e2e, "clocks": clk, "batched": batched,
     }
     if not args.no_cpu_baseline:
         log("cpu baseline")
