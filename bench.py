@@ -51,6 +51,7 @@ def parse_args():
     ap.add_argument("--workers", type=int, default=12, help="concurrent engine contexts")
     ap.add_argument("--wave", type=int, default=12, help="chromosome launches per step")
     ap.add_argument("--smem-budget", type=int, default=None, help="shared memory per cell (bytes)")
+    ap.add_argument("--carveout", type=int, default=None, help="shared-memory carveout percent")
     ap.add_argument("--batched", type=int, default=1, help="also time the one-launch batched engine")
     return ap.parse_args()
 
@@ -254,7 +255,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     from modlefork_gb300 import build as mbuild
     from modlefork_gb300 import engine
-    from modlefork_gb300.simulate import CONCURRENT_SMEM_BUDGET
+    from modlefork_gb300.simulate import CONCURRENT_CARVEOUT, CONCURRENT_SMEM_BUDGET
 
     mbuild.build()
     cfg, tasks = build_workload(args.cells, rank)
@@ -262,6 +263,7 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     budget = args.smem_budget if args.smem_budget is not None else (
         0 if args.workers == 1 else CONCURRENT_SMEM_BUDGET)
+    carveout = args.carveout if args.carveout is not None else (0 if args.workers == 1 else CONCURRENT_CARVEOUT)
     for t in tasks:
         t["d_seeds"] = torch.from_numpy(t["seeds"].view(np.int64)).to(dev)
         t["d_targets"] = torch.from_numpy(t["targets"].view(np.int64)).to(dev)
@@ -269,7 +271,7 @@ def run_ours(args):
     workers = []
     for _ in range(args.workers):
         eng = engine.Engine(cfg, local)
-        eng.set_debug_flags(0, budget)
+        eng.set_debug_flags((carveout & 0xFF) << 8, budget)
         stream = torch.cuda.Stream(device=dev)
         eng.set_stream(stream.cuda_stream)
         cids = [eng.upload_chrom(t["chrom"], t["bars"]) for t in tasks]
@@ -404,7 +406,7 @@ def run_ours(args):
         bdt = time.perf_counter() - t0
         batched = {"value": ble / (bms / 1e3), "unit": "LEF-epochs/s", "ms": bms, "launches": 1,
                    "cells_per_s": len(bst) / (bms / 1e3),
-                   "config": "the same 24 chromosomes x 512 cells in one batched launch, 32 KiB per cell",
+                   "config": "the same 24 chromosomes x 512 cells in one batched launch, 16 KiB per cell, 60% carveout",
                    "e2e": {"value": sum(x.lef_epochs for x in bst2) / bdt, "unit": "LEF-epochs/s",
                            "h2d_bytes_per_step": int(sum(b.nbytes for b in hb.values()) + len(btasks) * 40),
                            "d2h_bytes_per_step": int(sum(b.nbytes for b in hb.values()) + len(btasks) * 64)}}
@@ -425,7 +427,7 @@ def run_ours(args):
                            f"{args.workers} concurrent contexts; step i covers chromosomes "
                            f"{wave}i..{wave}i+{wave - 1} mod {len(tasks)}",
                    "timed_chromosomes": [tasks[k]["chrom"].name for k in timed],
-                   "workers": args.workers, "smem_budget_per_cell": budget,
+                   "workers": args.workers, "smem_budget_per_cell": budget, "smem_carveout_pct": carveout,
                    "genome_bp": int(sum(t["chrom"].size for t in tasks)),
                    "lefs": int(sum(t["nlefs"] for t in tasks)),
                    "barriers": int(sum(len(t["bars"]) for t in tasks)),

@@ -232,10 +232,12 @@ int mgpu_last_kernel_ms(mgpu_ctx* ctx, double* ms);
  * move adjustment, bit 2 collision processing, bit 3 contact sampling use the exact serial
  * restatement instead of the warp-parallel form (results are identical either way);
  * smem_budget caps the shared memory one cell may use (0 = device limit), placing the
- * remaining per-LEF arrays in global scratch. */
+ * remaining per-LEF arrays in global scratch.  Flags bits 8-15 give the shared-memory carveout
+ * preference in percent and bits 16-23 cap the cells per SM (0 = the driver's default and the
+ * occupancy limit). */
 int mgpu_set_debug_flags(mgpu_ctx* ctx, uint32_t flags, uint64_t smem_budget);
 
-/* Profile of the last mgpu_simulate_cells launch (no counterpart in the reference): SM cycles
+/* Profile of the last mgpu_simulate_cells or mgpu_simulate_batch launch (no counterpart in the reference): SM cycles
  * spent in each step of the epoch summed over cells (entries 0-15: burn-in, bind, rank,
  * contacts, moves, adjust, barriers, boundaries, LEF-BAR, primary, corrections, secondary,
  * fix, extrude+release, trace, total) and event counts (16: rank fallbacks, 17: adjust
@@ -378,7 +380,8 @@ int mgpu_simulate_cells_ex(mgpu_ctx* ctx, int chrom_id, const uint64_t* cell_see
  * chromosome) receives the contacts, added to; missed[chrom_id] is incremented (may be NULL);
  * stats[i] is task i's outcome (may be NULL).  Results equal one mgpu_simulate_cells call per
  * chromosome.  A shared-memory budget set with mgpu_set_debug_flags applies to every cell;
- * without one, large batches use 32 KiB per cell so that many cells share an SM.
+ * without one, large batches use 16 KiB per cell and a 60 % shared-memory carveout, so that
+ * eight cells share an SM and keep a large L1 for their arrays in global slots.
  */
 typedef struct mgpu_batch_task {
   uint64_t seed;

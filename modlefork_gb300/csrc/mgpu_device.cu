@@ -2891,6 +2891,11 @@ u64 max_smem_per_block() {
 }
 
 u64 resident_cells(const KParams& P, u64 ncells) {
+  // tuning switches carried in the debug flags: bits 8-15 carveout percent, 16-23 cells per SM
+  const u32 carveout = (P.debug_flags >> 8) & 0xFFu, max_per_sm = (P.debug_flags >> 16) & 0xFFu;
+  cudaFuncSetAttribute(simulate_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                       carveout ? (int)carveout : -1);
+  cudaGetLastError();
   // The attribute is a per-function permission shared by every thread and context of the
   // process, so it is always set to the device limit: lowering it for one launch would make a
   // concurrent launch with a larger plan fail.
@@ -2942,29 +2947,36 @@ int launch_simulate(const KParams& P, const DevChrom& ch, const CellTask* tasks,
   return cuda_fail(cudaGetLastError(), "simulate_kernel launch", errbuf, errlen);
 }
 
-u64 resident_batch_cells(u32 smem_bytes, u64 ntasks) {
+u64 resident_batch_cells(u32 smem_bytes, u64 ntasks, u32 carveout_pct, u32 max_per_sm) {
   if (cudaFuncSetAttribute(simulate_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)max_smem_per_block()) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
+  // shared memory / L1 split preference (a tuning switch; -1 lets the driver choose)
+  cudaFuncSetAttribute(simulate_batch_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                       carveout_pct ? (int)carveout_pct : -1);
+  cudaGetLastError();
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, simulate_batch_kernel, 32, smem_bytes) !=
       cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
+  if (max_per_sm && per_sm > (int)max_per_sm) per_sm = (int)max_per_sm;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (max_per_sm && per_sm > (int)max_per_sm) per_sm = (int)max_per_sm;
   const u64 grid = (u64)sms * (u64)(per_sm > 0 ? per_sm : 1);
   return grid < ntasks ? grid : ntasks;
 }
 
 int launch_simulate_batch(const BatchPlan* plans, const BatchTask* tasks, u64 ntasks, u32 smem_bytes,
                           u64 slot_bytes, mgpu_cell_stats* stats, const void* jump_table, u32* work_counter,
-                          char* gscratch, u64 gscratch_bytes, void* stream, char* errbuf, int errlen) {
-  u64 grid = resident_batch_cells(smem_bytes, ntasks);
+                          char* gscratch, u64 gscratch_bytes, u32 carveout_pct, u32 max_per_sm, void* stream,
+                          char* errbuf, int errlen) {
+  u64 grid = resident_batch_cells(smem_bytes, ntasks, carveout_pct, max_per_sm);
   if (grid == 0) return ntasks ? MGPU_ERR_CUDA : MGPU_OK;
   if (slot_bytes && gscratch_bytes / slot_bytes < grid) grid = gscratch_bytes / slot_bytes;
   if (grid == 0) {

@@ -1079,8 +1079,11 @@ extern "C" int mgpu_simulate_batch(mgpu_ctx* ctx, const mgpu_batch_task* tasks, 
   }
   int dev_sms = 0;
   cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
-  const uint64_t budget = ctx->smem_budget ? ctx->smem_budget
-                                           : (ntasks >= 8ull * (uint64_t)dev_sms ? 32768ull : 0ull);
+  // Large batches: 16 KiB per cell and a 60 % shared-memory carveout, so that eight cells share
+  // an SM and the per-LEF arrays that live in global slots keep a large L1 (measured best on the
+  // genome workload).
+  const bool large = ntasks >= 8ull * (uint64_t)dev_sms;
+  const uint64_t budget = ctx->smem_budget ? ctx->smem_budget : (large ? 16384ull : 0ull);
   std::vector<BatchPlan> plans(keys.size());
   u32 smem_bytes = 0;
   u64 slot_bytes = 0;
@@ -1109,8 +1112,9 @@ extern "C" int mgpu_simulate_batch(mgpu_ctx* ctx, const mgpu_batch_task* tasks, 
   for (size_t p = 0; p < keys.size(); ++p) {
     plans[p].band = (u32*)dband[keys[p].chrom].p;
     plans[p].missed = (unsigned long long*)d_missed.p + p;
-    plans[p].P.prof = nullptr;
+    plans[p].P.prof = ctx->d_prof;
   }
+  CK(cudaMemsetAsync(ctx->d_prof, 0, 32 * sizeof(uint64_t), st));
   // work queue: largest LEF count first, cells of one plan together
   std::vector<uint64_t> order(ntasks);
   for (uint64_t i = 0; i < ntasks; ++i) order[i] = i;
@@ -1132,17 +1136,21 @@ extern "C" int mgpu_simulate_batch(mgpu_ctx* ctx, const mgpu_batch_task* tasks, 
   if (rc) return rc;
   CK(cudaMemcpyAsync(d_plans.p, plans.data(), plans.size() * sizeof(BatchPlan), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d_tasks.p, bt.data(), ntasks * sizeof(BatchTask), cudaMemcpyHostToDevice, st));
+  // tuning switches (mgpu_set_debug_flags bits 8-15: carveout percent, 16-23: blocks per SM cap)
+  u32 carveout = (ctx->debug_flags >> 8) & 0xFFu;
+  const u32 max_per_sm = (ctx->debug_flags >> 16) & 0xFFu;
+  if (!carveout && large && !ctx->smem_budget) carveout = 60;
   if (slot_bytes) {
     KParams Pslot = plans[0].P;
     Pslot.slot_bytes = slot_bytes;
-    rc = ensure_scratch(ctx, Pslot, resident_batch_cells(smem_bytes, ntasks));
+    rc = ensure_scratch(ctx, Pslot, resident_batch_cells(smem_bytes, ntasks, carveout, max_per_sm));
     if (rc) return rc;
   }
   char err[256] = {0};
   CK(cudaEventRecord(ctx->ev0, st));
   rc = launch_simulate_batch((const BatchPlan*)d_plans.p, (const BatchTask*)d_tasks.p, ntasks, smem_bytes,
                              slot_bytes, (mgpu_cell_stats*)d_stats.p, ctx->d_jump, ctx->d_work, ctx->d_scratch,
-                             ctx->scratch_bytes, st, err, sizeof(err));
+                             ctx->scratch_bytes, carveout, max_per_sm, st, err, sizeof(err));
   if (rc) return fail(rc, "%s", err);
   CK(cudaEventRecord(ctx->ev1, st));
   for (auto& kv : dband) {
@@ -1158,6 +1166,7 @@ extern "C" int mgpu_simulate_batch(mgpu_ctx* ctx, const mgpu_batch_task* tasks, 
   std::vector<mgpu_cell_stats> h_stats(ntasks);
   CK(cudaMemcpyAsync(h_missed.data(), d_missed.p, keys.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(h_stats.data(), d_stats.p, ntasks * sizeof(mgpu_cell_stats), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(ctx->h_prof, ctx->d_prof, 32 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   {
     float ms = 0.f;

@@ -208,9 +208,11 @@ struct BatchTask {
 };
 int launch_simulate_batch(const BatchPlan* plans, const BatchTask* tasks, u64 ntasks, u32 smem_bytes,
                           u64 slot_bytes, mgpu_cell_stats* stats, const void* jump_table, u32* work_counter,
-                          char* gscratch, u64 gscratch_bytes, void* stream, char* errbuf, int errlen);
-// Grid of a batched launch with the given per-cell shared memory.
-u64 resident_batch_cells(u32 smem_bytes, u64 ntasks);
+                          char* gscratch, u64 gscratch_bytes, u32 carveout_pct, u32 max_per_sm, void* stream,
+                          char* errbuf, int errlen);
+// Grid of a batched launch with the given per-cell shared memory (optionally capped per SM, with
+// a shared-memory carveout preference in percent, 0 = driver default).
+u64 resident_batch_cells(u32 smem_bytes, u64 ntasks, u32 carveout_pct = 0, u32 max_per_sm = 0);
 
 // Pixel table of a band (mgpu_pixels.cu): counts[i] = non-zero pixels of bin1 row i,
 // offsets[0..ncols] their exclusive scan; then the (bin1, bin2, count) pixels.

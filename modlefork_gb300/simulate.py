@@ -45,9 +45,11 @@ def prepare_chrom(eng, cfg, chrom, barriers, ncells):
                 seeds=seeds, nrows=nrows, ncols=ncols)
 
 
-# Shared-memory budget per cell when several chromosome launches run at once: enough for the
-# hottest per-LEF arrays of a mid-sized chromosome while about seven cells fit on an SM.
-CONCURRENT_SMEM_BUDGET = 32 * 1024
+# Shared-memory budget per cell when several chromosome launches run at once, and the share of
+# the SM's unified memory given to shared memory (the rest is L1 for the per-LEF arrays that
+# live in global slots): six cells per SM with a 70 KB L1 measured best on the genome workload.
+CONCURRENT_SMEM_BUDGET = 24 * 1024
+CONCURRENT_CARVEOUT = 70
 
 
 def simulate_genome(cfg, genome, ncells=None, device=0, simulate_wo_barriers=False, workers=1,
@@ -74,7 +76,7 @@ def simulate_genome(cfg, genome, ncells=None, device=0, simulate_wo_barriers=Fal
     def worker():
         try:
             with engine.Engine(cfg, device) as eng:
-                eng.set_debug_flags(0, smem_budget)
+                eng.set_debug_flags((CONCURRENT_CARVEOUT << 8) if workers > 1 else 0, smem_budget)
                 while True:
                     try:
                         i, chrom, barriers = todo.get_nowait()
