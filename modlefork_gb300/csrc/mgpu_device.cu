@@ -1098,15 +1098,26 @@ __device__ bool rank_dir_split(Cell& c, u32 dir, u32 n) {
   u32* ev_rd = c.sf + 2 * EMAX;
   u32* B = c.tmp;
   const u32 lane = ln();
+  // positions in input order, gathered up front with independent loads (B is written to tmp
+  // only after the pass)
+  {
+    const u32* __restrict__ Rr = R;
+    const u32* __restrict__ pr = pos;
+    u32* __restrict__ V = c.tmp;
+#pragma unroll 4
+    for (u32 r = lane; r < n; r += 32) V[r] = pr[Rr[r]];
+  }
+  __syncwarp();
+  const u32* V = c.tmp;
   const u32 first = R[0];
   if (lane == 0) K[0] = first;
-  u32 m = 0, T = pos[first], E = 0, q = 0;
+  u32 m = 0, T = V[0], E = 0, q = 0;
   for (u32 base = 1; base < n; base += 32) {
     const u32 r = base + lane;
     const u32 nvalid = min(32u, n - base);
     const bool valid = lane < nvalid;
     const u32 idx = valid ? R[r] : 0;
-    const u32 v = valid ? pos[idx] : 0;
+    const u32 v = valid ? V[r] : 0;
     const u32 vprev = __shfl_up_sync(FULL, v, 1);
     const bool pre_ok = lane == 0 || v >= vprev;
     u32 start = 0;
@@ -1208,14 +1219,16 @@ __device__ bool rank_dir_split(Cell& c, u32 dir, u32 n) {
     __syncwarp();
     Bf = B;
   }
-  // tie fix of K: runs of equal positions whose epochs are out of order
+  // tie fix of K: runs of equal positions whose epochs are out of order (each element's key is
+  // read once; the previous element's comes from the adjacent lane or the previous chunk)
+  u64 kprev = ns ? rank_key(c, dir, K[0]) : 0;
   for (u32 base = 1; base < ns; base += 32) {
     const u32 t = base + lane;
-    bool bad = false;
-    if (t < ns) {
-      const u32 a0 = K[t - 1], a1 = K[t];
-      bad = pos[a0] == pos[a1] && rank_key(c, dir, a0) > rank_key(c, dir, a1);
-    }
+    const u64 kt = t < ns ? rank_key(c, dir, K[t]) : ~0ull;
+    u64 k0 = __shfl_up_sync(FULL, kt, 1);
+    if (lane == 0) k0 = kprev;
+    kprev = __shfl_sync(FULL, kt, 31);
+    const bool bad = t < ns && (k0 >> 32) == (kt >> 32) && k0 > kt;
     unsigned bm = __ballot_sync(FULL, bad);
     if (bm) {
       if (lane == 0) {
@@ -1227,6 +1240,9 @@ __device__ bool rank_dir_split(Cell& c, u32 dir, u32 n) {
         }
       }
       __syncwarp();
+      // a fixed run may reach the chunk's end: carry the key now at its last slot
+      const u32 tl = min(base + 31, ns - 1);
+      kprev = rank_key(c, dir, K[tl]);
     }
   }
   // merge, K first among equal keys.  u_j = #K with key <= key(B_j) (binary search; K is
@@ -1277,9 +1293,16 @@ __device__ void rank_lefs(Cell& c, const KParams& P, u32 n, u32 epoch, bool part
 
 // positions in rank order: sr[k] = rev[rr[k]], sf[k] = fwd[fr[k]]
 __device__ void gather_ranked(Cell& c, u32 n) {
+  const u32* __restrict__ rr = c.rr;
+  const u32* __restrict__ fr = c.fr;
+  const u32* __restrict__ rev = c.rev;
+  const u32* __restrict__ fwd = c.fwd;
+  u32* __restrict__ sr = c.sr;
+  u32* __restrict__ sf = c.sf;
+#pragma unroll 4
   for (u32 k = ln(); k < n; k += 32) {
-    c.sr[k] = c.rev[c.rr[k]];
-    c.sf[k] = c.fwd[c.fr[k]];
+    sr[k] = rev[rr[k]];
+    sf[k] = fwd[fr[k]];
   }
   __syncwarp();
 }
@@ -1409,6 +1432,7 @@ __device__ bool adjust_rev_fast(Cell& c, const KParams& P, u32 n) {
   }
   if (__any_sync(FULL, bad)) return false;
   __syncwarp();
+#pragma unroll 4
   for (u32 k = ln(); k < n; k += 32) c.rm[c.rr[k]] = out[k];
   __syncwarp();
   return true;
@@ -1454,6 +1478,7 @@ __device__ bool adjust_fwd_fast(Cell& c, const KParams& P, u32 n) {
   }
   if (__any_sync(FULL, bad)) return false;
   __syncwarp();
+#pragma unroll 4
   for (u32 k = ln(); k < n; k += 32) c.fm[c.fr[k]] = out[k];
   __syncwarp();
   return true;
@@ -1475,12 +1500,19 @@ __device__ void adjust_moves(Cell& c, const KParams& P, u32 n) {
 
 // clamp_moves (simulation.cpp:325-340)
 __device__ void clamp_moves(Cell& c, const KParams& P, u32 n) {
+  const u32* __restrict__ bep = c.bep;
+  const u32* __restrict__ rev = c.rev;
+  const u32* __restrict__ fwd = c.fwd;
+  u32* __restrict__ rm = c.rm;
+  u32* __restrict__ fm = c.fm;
+  const u64 start = P.start, end = P.end;
+#pragma unroll 4
   for (u32 i = ln(); i < n; i += 32) {
-    if (c.bep[i] == UNBOUND) continue;
-    const u64 rmv = min((u64)c.rm[i], pos64(c.rev[i]) - P.start);
-    const u64 fmv = min((u64)c.fm[i], (u64)P.end - pos64(c.fwd[i]) - 1);
-    c.rm[i] = (u32)rmv;
-    c.fm[i] = (u32)fmv;
+    if (bep[i] == UNBOUND) continue;
+    const u64 rmv = min((u64)rm[i], pos64(rev[i]) - start);
+    const u64 fmv = min((u64)fm[i], end - pos64(fwd[i]) - 1);
+    rm[i] = (u32)rmv;
+    fm[i] = (u32)fmv;
   }
   __syncwarp();
 }
@@ -1489,8 +1521,18 @@ __device__ void clamp_moves(Cell& c, const KParams& P, u32 n) {
 // always satisfies it, caller-provided ranks may not.
 __device__ bool ranked_sorted(const Cell& c, u32 n) {
   bool bad = false;
-  for (u32 k = ln() + 1; k < n; k += 32) {
-    if (c.sr[k - 1] > c.sr[k] || c.sf[k - 1] > c.sf[k]) bad = true;
+  u32 pr = 0, pf = 0;  // last values of the previous chunk
+  for (u32 base = 0; base < n; base += 32) {
+    const u32 k = base + ln();
+    const u32 r = k < n ? c.sr[k] : UNBOUND, f = k < n ? c.sf[k] : UNBOUND;
+    u32 r0 = __shfl_up_sync(FULL, r, 1), f0 = __shfl_up_sync(FULL, f, 1);
+    if (ln() == 0) {
+      r0 = pr;
+      f0 = pf;
+    }
+    if (k < n && k > 0 && (r0 > r || f0 > f)) bad = true;
+    pr = __shfl_sync(FULL, r, 31);
+    pf = __shfl_sync(FULL, f, 31);
   }
   return !__any_sync(FULL, bad);
 }
@@ -1691,10 +1733,17 @@ __device__ void detect_primary_fast(Cell& c, u64* s, const KParams& P, u32 n, u6
 
 // correct_moves_for_lef_bar_collisions (simulation_correct_moves.cpp:20-51)
 __device__ void correct_lef_bar(Cell& c, u32 n) {
+  const u32* __restrict__ rc = c.rc;
+  const u32* __restrict__ fc = c.fc;
+  const u32* __restrict__ rev = c.rev;
+  const u32* __restrict__ fwd = c.fwd;
+  u32* __restrict__ rm = c.rm;
+  u32* __restrict__ fm = c.fm;
+#pragma unroll 4
   for (u32 i = ln(); i < n; i += 32) {
-    const u32 r = c.rc[i], f = c.fc[i];
-    if (cw_occurred_as(r, EV_LEF_BAR)) c.rm[i] = (u32)(pos64(c.rev[i]) - bar_pos(c, cw_idx(r)) - 1);
-    if (cw_occurred_as(f, EV_LEF_BAR)) c.fm[i] = (u32)(bar_pos(c, cw_idx(f)) - pos64(c.fwd[i]) - 1);
+    const u32 r = rc[i], f = fc[i];
+    if (cw_occurred_as(r, EV_LEF_BAR)) rm[i] = (u32)(pos64(rev[i]) - bar_pos(c, cw_idx(r)) - 1);
+    if (cw_occurred_as(f, EV_LEF_BAR)) fm[i] = (u32)(bar_pos(c, cw_idx(f)) - pos64(fwd[i]) - 1);
   }
   __syncwarp();
 }
@@ -1798,19 +1847,32 @@ __device__ void secondary_dir_fast(Cell& c, u64* s, const KParams& P, u32 dir, u
   // and R[k] free, in descending i
   u32* starts = c.tmp;
   u32 nst = 0;
+  // stalled(k) = the unit of rank k collided; each unit's word is read once and its neighbour's
+  // flag comes from the adjacent lane (or the previous chunk)
   if (dir == 0) {
-    for (u32 base = (u32)max((u64)1, n5); base < n; base += 32) {
+    const u32 k0 = (u32)max((u64)1, n5);
+    bool prev = k0 - 1 < n && cw_occurred(C[R[k0 - 1]]);
+    for (u32 base = k0; base < n; base += 32) {
       const u32 k = base + ln();
-      const bool st = k < n && cw_occurred(C[R[k - 1]]) && !cw_occurred(C[R[k]]);
+      const bool cur = k < n && cw_occurred(C[R[k]]);
+      bool before = __shfl_up_sync(FULL, cur, 1);
+      if (ln() == 0) before = prev;
+      const bool st = k < n && before && !cur;
       const unsigned m = __ballot_sync(FULL, st);
       if (st) starts[nst + __popc(m & lanemask_lt())] = k;
       nst += __popc(m);
+      prev = __shfl_sync(FULL, cur, 31);
     }
   } else {
     const i64 itop = (i64)(n - min(n3, n3 - 1)) - 1;
     for (i64 top = itop; top >= 1; top -= 32) {
+      // lane l holds i = top - l and needs stalled(i) and stalled(i - 1): the latter is the
+      // next lane's flag, read directly by lane 31
       const i64 i = top - (i64)ln();
-      const bool st = i >= 1 && cw_occurred(C[R[i]]) && !cw_occurred(C[R[i - 1]]);
+      const bool stalled = i >= 0 && cw_occurred(C[R[i]]);
+      bool below = __shfl_down_sync(FULL, stalled, 1);
+      if (ln() == 31) below = i - 1 >= 0 && cw_occurred(C[R[i - 1]]);
+      const bool st = i >= 1 && stalled && !below;
       const unsigned m = __ballot_sync(FULL, st);
       if (st) starts[nst + __popc(m & lanemask_lt())] = (u32)(i - 1);
       nst += __popc(m);
@@ -1955,10 +2017,16 @@ __device__ void process_collisions(Cell& c, u64* s, const KParams& P, u32 n, boo
 
 // extrude (simulation.cpp:489-512)
 __device__ void extrude(Cell& c, u32 n) {
+  const u32* __restrict__ bep = c.bep;
+  const u32* __restrict__ rm = c.rm;
+  const u32* __restrict__ fm = c.fm;
+  u32* __restrict__ rev = c.rev;
+  u32* __restrict__ fwd = c.fwd;
+#pragma unroll 4
   for (u32 i = ln(); i < n; i += 32) {
-    if (c.bep[i] == UNBOUND) continue;
-    c.rev[i] -= c.rm[i];
-    c.fwd[i] += c.fm[i];
+    if (bep[i] == UNBOUND) continue;
+    rev[i] -= rm[i];
+    fwd[i] += fm[i];
   }
   __syncwarp();
 }
@@ -2011,6 +2079,7 @@ __device__ bool burnin_stats(Cell& c, const KParams& P, u32 n) {
     return false;
   }
   u64 part = 0;
+#pragma unroll 4
   for (u32 i = ln(); i < n; i += 32) part += pos64(c.fwd[i]) - pos64(c.rev[i]);
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) part += __shfl_xor_sync(FULL, part, d);
@@ -2596,6 +2665,7 @@ __device__ void run_cell(Cell& c, u64* s, const KParams& P, const CellTask& task
     ta = clock64();
     prof_add(c, PF_ADJUST, ta - tb);
     barriers_next(c, s);
+#pragma unroll 4
     for (u32 i = ln(); i < n; i += 32) {
       c.rc[i] = 0;
       c.fc[i] = 0;
