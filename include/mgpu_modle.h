@@ -230,14 +230,16 @@ int mgpu_last_kernel_ms(mgpu_ctx* ctx, double* ms);
 
 /* Test and tuning switches (no counterpart in the reference).  flags: bit 0 ranks, bit 1
  * move adjustment, bit 2 collision processing, bit 3 contact sampling use the exact serial
- * restatement instead of the warp-parallel form (results are identical either way);
+ * restatement instead of the warp-parallel form (results are identical either way); bit 4
+ * collects the per-step cycle counters of mgpu_last_profile;
  * smem_budget caps the shared memory one cell may use (0 = device limit), placing the
  * remaining per-LEF arrays in global scratch.  Flags bits 8-15 give the shared-memory carveout
  * preference in percent and bits 16-23 cap the cells per SM (0 = the driver's default and the
  * occupancy limit). */
 int mgpu_set_debug_flags(mgpu_ctx* ctx, uint32_t flags, uint64_t smem_budget);
 
-/* Profile of the last mgpu_simulate_cells or mgpu_simulate_batch launch (no counterpart in the reference): SM cycles
+/* Profile of the last mgpu_simulate_cells or mgpu_simulate_batch launch made with debug flag
+ * bit 4 (all zero otherwise; no counterpart in the reference): SM cycles
  * spent in each step of the epoch summed over cells (entries 0-15: burn-in, bind, rank,
  * contacts, moves, adjust, barriers, boundaries, LEF-BAR, primary, corrections, secondary,
  * fix, extrude+release, trace, total) and event counts (16: rank fallbacks, 17: adjust

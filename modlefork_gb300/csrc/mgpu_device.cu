@@ -88,7 +88,8 @@ enum : u32 {
   PF_BURNIN = 0, PF_BIND, PF_RANK, PF_CONTACTS, PF_MOVES, PF_ADJUST, PF_BARRIERS, PF_BOUNDARIES,
   PF_LEF_BAR, PF_PRIMARY, PF_CORRECT, PF_SECONDARY, PF_FIX, PF_EXTRUDE_RELEASE, PF_TRACE, PF_TOTAL,
   PF_RANK_FALLBACK, PF_ADJUST_FALLBACK, PF_CHAIN_SERIAL, PF_CONTACT_SERIAL, PF_FIX_FALLBACK,
-  PF_REFILLS, PF_STALE_REFILLS, PF_EPOCHS, PF_RANK_PDQ, PF_COUNT = 32
+  PF_REFILLS, PF_STALE_REFILLS, PF_EPOCHS, PF_RANK_PDQ, PF_RANK_PASS, PF_RANK_BLOCK, PF_RANK_MERGE,
+  PF_COUNT = 32
 };
 
 struct Scalars {
@@ -1098,6 +1099,7 @@ __device__ bool rank_dir_split(Cell& c, u32 dir, u32 n) {
   u32* ev_rd = c.sf + 2 * EMAX;
   u32* B = c.tmp;
   const u32 lane = ln();
+  u64 tprof = clock64();
   // positions in input order, gathered up front with independent loads (B is written to tmp
   // only after the pass)
   {
@@ -1152,6 +1154,11 @@ __device__ bool rank_dir_split(Cell& c, u32 dir, u32 n) {
     }
   }
   __syncwarp();
+  {
+    const u64 t = clock64();
+    prof_add(c, PF_RANK_PASS, t - tprof);
+    tprof = t;
+  }
   const u32 ns = m + 1;
   // block size before each event, and the rotation it saw since the previous event
   u32 kacc = 0;
@@ -1219,6 +1226,11 @@ __device__ bool rank_dir_split(Cell& c, u32 dir, u32 n) {
     __syncwarp();
     Bf = B;
   }
+  {
+    const u64 t = clock64();
+    prof_add(c, PF_RANK_BLOCK, t - tprof);
+    tprof = t;
+  }
   // tie fix of K: runs of equal positions whose epochs are out of order (each element's key is
   // read once; the previous element's comes from the adjacent lane or the previous chunk)
   u64 kprev = ns ? rank_key(c, dir, K[0]) : 0;
@@ -1274,6 +1286,7 @@ __device__ bool rank_dir_split(Cell& c, u32 dir, u32 n) {
     jb = j;
   }
   __syncwarp();
+  prof_add(c, PF_RANK_MERGE, clock64() - tprof);
   return true;
 }
 

@@ -982,7 +982,7 @@ static int run_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* seeds, const u
     P.rec_max = rec_max;
     P.rec_count = (u64*)d_recn.p;
   }
-  P.prof = ctx->d_prof;
+  P.prof = (ctx->debug_flags & DBG_PROFILE) ? ctx->d_prof : nullptr;
   CK(cudaMemsetAsync(ctx->d_prof, 0, 32 * sizeof(uint64_t), st));
   CK(cudaEventRecord(ctx->ev0, st));
   rc = launch_simulate(P, dc, (const CellTask*)d_tasks.p, ncells, target_epochs, (u32*)d_band.p,
@@ -1112,7 +1112,7 @@ extern "C" int mgpu_simulate_batch(mgpu_ctx* ctx, const mgpu_batch_task* tasks, 
   for (size_t p = 0; p < keys.size(); ++p) {
     plans[p].band = (u32*)dband[keys[p].chrom].p;
     plans[p].missed = (unsigned long long*)d_missed.p + p;
-    plans[p].P.prof = ctx->d_prof;
+    plans[p].P.prof = (ctx->debug_flags & DBG_PROFILE) ? ctx->d_prof : nullptr;
   }
   CK(cudaMemsetAsync(ctx->d_prof, 0, 32 * sizeof(uint64_t), st));
   // work queue: largest LEF count first, cells of one plan together

@@ -132,6 +132,7 @@ enum : u32 {
   DBG_SERIAL_ADJUST = 1u << 1,
   DBG_SERIAL_COLLISIONS = 1u << 2,
   DBG_SERIAL_CONTACTS = 1u << 3,
+  DBG_PROFILE = 1u << 4,  // collect per-step cycle counters (mgpu_last_profile)
 };
 
 struct CellTask {

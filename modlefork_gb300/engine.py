@@ -384,14 +384,16 @@ class Engine:
 
     def set_debug_flags(self, flags=0, smem_budget=0):
         """Force the serial restatement of some steps (bit 0 rank, 1 adjust, 2 collisions,
-        3 contacts) and/or cap a cell's shared memory (bytes, 0 = device limit)."""
+        3 contacts), collect the step profile (bit 4), set the carveout (bits 8-15) and the
+        cells-per-SM cap (bits 16-23), and/or cap a cell's shared memory (bytes, 0 = limit)."""
         _check(self.lib.mgpu_set_debug_flags(self.h, flags, smem_budget), "mgpu_set_debug_flags")
 
     PROFILE_NAMES = ("burnin", "bind", "rank", "contacts", "moves", "adjust", "barriers",
                      "boundaries", "lef_bar", "primary", "correct", "secondary", "fix",
                      "extrude_release", "trace", "total", "rank_fallbacks", "adjust_fallbacks",
                      "serial_chain_walks", "serial_contact_attempts", "fix_fallbacks", "refills",
-                     "stale_refills", "epochs", "rank_pdq")
+                     "stale_refills", "epochs", "rank_pdq", "rank_pass", "rank_block",
+                     "rank_merge")
 
     def last_profile(self):
         buf = (C.c_uint64 * 32)()
