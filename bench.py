@@ -3,9 +3,9 @@
 
 Workload: 24 synthetic chromosomes, lengths uniform in [50, 250] Mbp, 5 kb bins, 3 Mbp band,
 one barrier per 50 kb (Beta(8, 2) occupancy), 20 LEFs/Mbp, 200 kb lifetime, 512 cells per
-chromosome, contact density 1, one engine launch per chromosome.  One step is a wave of twelve
-such launches that run at once from twelve engine contexts (host threads, CUDA streams); step i
-covers chromosomes 12i..12i+11 mod 24, so the default 2 steps cover the genome once.  The metric is
+chromosome, contact density 1, one engine launch per chromosome.  One step is the whole genome:
+the 24 launches run at once from 24 engine contexts (host threads, CUDA streams), each cell
+with a 24 KiB shared-memory budget and a 70 % shared-memory carveout.  The metric is
 LEF-epochs/s (sum over cells and epochs of active LEFs, burn-in included), with cells/s and
 contacts/s reported beside it.
 
@@ -41,15 +41,15 @@ WORKLOAD = "genome_24chr_50-250Mbp_5kb_512cells"
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cells", type=int, default=512, help="cells per chromosome")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline time budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--workers", type=int, default=12, help="concurrent engine contexts")
-    ap.add_argument("--wave", type=int, default=12, help="chromosome launches per step")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--workers", type=int, default=24, help="concurrent engine contexts")
+    ap.add_argument("--wave", type=int, default=24, help="chromosome launches per step")
     ap.add_argument("--smem-budget", type=int, default=None, help="shared memory per cell (bytes)")
     ap.add_argument("--carveout", type=int, default=None, help="shared-memory carveout percent")
     ap.add_argument("--batched", type=int, default=1, help="also time the one-launch batched engine")
