@@ -1972,10 +1972,13 @@ __device__ bool fix_secondary_fast(Cell& c, const KParams& P, u32 n, u64 n5, u64
 }
 
 // process_collisions (simulation.cpp:925-955) in the reference's order.
-__device__ void process_collisions(Cell& c, u64* s, const KParams& P, u32 n, bool fix) {
+// sorted_ranks: the ranked positions are known to be sorted (the epoch loop ranks them itself);
+// otherwise (caller state) they are checked and unsorted ones take the serial restatement.
+__device__ void process_collisions(Cell& c, u64* s, const KParams& P, u32 n, bool fix,
+                                   bool sorted_ranks = false) {
   Scalars* sc = c.sc;
   u64 t0 = clock64();
-  const bool serial = (P.debug_flags & DBG_SERIAL_COLLISIONS) || !ranked_sorted(c, n);
+  const bool serial = (P.debug_flags & DBG_SERIAL_COLLISIONS) || !(sorted_ranks || ranked_sorted(c, n));
   __syncwarp();
   if (ln() == 0) {
     u64 n5, n3;
@@ -2686,7 +2689,7 @@ __device__ void run_cell(Cell& c, u64* s, const KParams& P, const CellTask& task
     __syncwarp();
     tb = clock64();
     prof_add(c, PF_BARRIERS, tb - ta);
-    process_collisions(c, s, P, n, true);
+    process_collisions(c, s, P, n, true, true);
     ta = clock64();
     extrude(c, n);
     if (P.log_state) log_model_state(c, P, n, cell);

@@ -151,6 +151,10 @@ STRESS = {
     "skip_burnin_epochs": (dict(skip_burnin=1, stop_on_epochs=1, target_simulation_epochs=300,
                                 num_cells=4), 2_000_000, 80, "beta"),
     "offset_start": (dict(), 3_000_000, 60, None),
+    # no barriers at all: LEF-BAR sweeps over an empty track
+    "no_barriers": (dict(), 2_000_000, 0, None),
+    # the 1D occupancy and model-state outputs enabled (more draws per epoch)
+    "outputs_on": (dict(track_1d_lef_position=1, log_model_internal_state=1), 2_000_000, 40, "beta"),
 }
 
 
@@ -277,6 +281,16 @@ def test_unreachable_contacts_end_with_timeout_status():
         with pytest.raises(engine.EngineError) as e:
             eng.simulate_cells(cid, np.array([1], dtype=np.uint64), np.array([10], dtype=np.uint64), 0, 4, band)
     assert e.value.code == abi.MGPU_ERR_TIMEOUT
+
+
+@pytest.mark.parametrize("mode", ["fast", "global_scratch"])
+def test_largest_genome_chromosome_cell(mode):
+    """The genome workload's largest chromosome (246 Mbp, 4918 LEFs and barriers): one whole
+    cell, every epoch, against the oracle."""
+    cfg, gen = genome.genome_24chr(seed=11)
+    chrom, bars = max(gen, key=lambda cb: cb[0].size)
+    assert chrom.size > 240_000_000
+    compare_cell(cfg, chrom, bars, cell_id=3, max_epochs=5000, mode=mode)
 
 
 @pytest.mark.parametrize("mode", list(MODES))
