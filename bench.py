@@ -128,12 +128,13 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def dram_traffic_per_launch():
-    """DRAM bytes per launch of the simulation kernel from the committed ncu summary."""
+def dram_traffic_per_launch(lef_epochs_per_launch):
+    """DRAM bytes per launch of the simulation kernel, from the committed ncu capture's bytes per
+    LEF-epoch (one launch of the same kernel and layout) scaled to this run's launches."""
     path = os.path.join(ROOT, "profiles", "simulate_kernel_traffic.json")
     if os.path.exists(path):
         d = json.load(open(path))
-        return d.get("bytes_per_launch"), d
+        return d["bytes_per_lef_epoch"] * lef_epochs_per_launch, d
     return None, None
 
 
@@ -415,7 +416,7 @@ def run_ours(args):
         return
     peak, peak_kind = measured_peak()
     achieved = agg["bytes"] / (ms / 1e3) / 1e9
-    traffic, _ = dram_traffic_per_launch()
+    traffic, _ = dram_traffic_per_launch(agg["lef_epochs"] / max(1, agg["launches"]))
     timed = sorted({(i * wave + j) % len(tasks) for i in range(args.steps) for j in range(wave)})
     line = {
         "metric": "LEF-epochs/s", "value": agg["lef_epochs"] / (ms / 1e3), "unit": "LEF-epochs/s",
@@ -439,7 +440,11 @@ def run_ours(args):
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": f"{peak_kind} hbm_gbs", "kernel": "simulate_kernel",
                      "bytes_model": "24*LEF_epochs + 6*barriers*epochs + 8*contacts, summed over the "
-                                    "launches of the timed region / region time (launches overlap)"},
+                                    "launches of the timed region / region time (launches overlap)",
+                     "traffic_note": "DRAM bytes per launch: ncu bytes per LEF-epoch of one launch "
+                                     "(profiles/simulate_kernel_traffic.json) x this run's LEF-epochs per "
+                                     "launch; far below the algorithmic bytes because the cells' state "
+                                     "stays on chip and in L2"},
         "e2e": e2e, "clocks": clk, "batched": batched,
     }
     if not args.no_cpu_baseline:
