@@ -30,7 +30,9 @@ def _stats_tuple(s):
     return (s.epochs, s.burnin_epochs, s.contacts, s.missed_updates, s.lef_epochs, s.rng_draws, s.status)
 
 
-def test_noalloc_twice_matches_simulate_cells():
+@pytest.mark.parametrize("smem_budget", [0, 12 * 1024])
+def test_noalloc_twice_matches_simulate_cells(smem_budget):
+    """Also with the per-LEF arrays in global cell slots, which then live in the fixed scratch."""
     torch = pytest.importorskip("torch")
     n = 24
     cfg, chrom, bars, nl, seeds, targets, te = _cells(n)
@@ -47,6 +49,7 @@ def test_noalloc_twice_matches_simulate_cells():
                          stats=torch.zeros(n * stat_bytes, dtype=torch.uint8, device=dev)))
     torch.cuda.synchronize()
     with engine.Engine(cfg) as eng:
+        eng.set_debug_flags(0, smem_budget)
         cid = eng.upload_chrom(chrom, bars)
         ref_missed, ref_stats = eng.simulate_cells(cid, seeds, targets, te, nl, ref_band)
         for o in outs:  # two calls in a row on the context's stream, no sync in between
