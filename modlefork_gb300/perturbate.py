@@ -10,8 +10,9 @@ the chromosome's hash of (seed, cell id) with cell ids counted per chromosome, i
 contact target follow from the window's size.
 
 Here every task becomes a window upload (mgpu_upload_window) and all tasks of a run advance in
-one batched launch (mgpu_simulate_batch).  The feature-pair scoring and bedpe output of the
-reference (reference cooler, block aggregation, binomial test) are not part of this module.
+one batched launch (mgpu_simulate_batch).  ``score_window`` then compares a window's contacts
+with a reference run's for every pair of features, as simulate_window's bedpe output does
+(block sums with edge extension, log2 ratio, two-sided binomial test).
 """
 
 import numpy as np
@@ -125,3 +126,94 @@ def simulate_windows(cfg, genome, deletion_size=10_000, features=None, device=0,
     for k, (chrom, t, cid) in enumerate(meta):
         results.append(WindowResult(chrom, t, bands[cid], stats[k]))
     return results
+
+
+# ---------------------------------------------------------------------------------------------
+# feature-pair scoring (Simulation::simulate_window, scheduler_perturbate.cpp:481-556)
+
+def band_get(band, nrows, ncols, i, j):
+    """ContactMatrixDense::unsafe_get: the count of bins (i, j), 0 outside the band."""
+    if i > j:
+        i, j = j, i
+    r = j - i
+    return 0 if r >= nrows else int(band[j * nrows + r])
+
+
+def band_block(band, nrows, ncols, row, col, block_size):
+    """ContactMatrixDense::unsafe_get_block (contact_matrix_dense_unsafe_impl.hpp:89-113): sum of
+    the block_size x block_size pixels centred on (row, col), edges extended."""
+    if block_size == 1:
+        return band_get(band, nrows, ncols, row, col)
+    h = block_size // 2
+    tot = 0
+    for i in range(row - h, row - h + block_size):
+        for j in range(col - h, col - h + block_size):
+            tot += band_get(band, nrows, ncols, min(max(i, 0), ncols - 1), min(max(j, 0), ncols - 1))
+    return tot
+
+
+def window_band_of(cfg, band, nrows_full, window_start, window_end):
+    """The reference run's contacts (a chromosome band with ``nrows_full`` rows) restricted to a
+    window, in the window's own band layout (read_reference_contacts,
+    scheduler_perturbate.cpp:76-87): pixels with both bins inside the window."""
+    bin_size = int(cfg.bin_size)
+    b0 = window_start // bin_size
+    nrows_w, ncols_w = engine.band_shape(cfg, window_end - window_start)
+    full = np.asarray(band).reshape(-1, nrows_full)
+    out = np.zeros((ncols_w, nrows_w), dtype=np.uint32)
+    for jr in range(max(0, min(ncols_w, full.shape[0] - b0))):
+        r = np.arange(min(nrows_w, nrows_full, jr + 1))
+        out[jr, r] = full[b0 + jr, r]
+    return out.reshape(-1)
+
+
+def binomial_test(k, n, p=0.5):
+    """stats::binomial_test, two-sided (src/stats/tests_impl.hpp:17-110), which follows scipy's
+    binomtest."""
+    from scipy.stats import binomtest
+
+    if n == 0:
+        return 1.0
+    return float(binomtest(int(k), int(n), p, alternative="two-sided").pvalue)
+
+
+def score_window(cfg, result, ref_window_band, feats1, feats2, block_size=9, last_window=False):
+    """bedpe records of one (window, deletion) task: for feature i of kind 1 and j >= i of kind
+    2 (each (chrom, start, end, name, strand)), the block sums of the window's and the
+    reference's contacts around their bins, their log2 ratio and binomial p-value, and the task's
+    window, deletion and barrier counts.  Pairs with both features past the partition point are
+    left to the next window (except in the last one), and pairs without contacts are skipped."""
+    t = result.task
+    ws, we = t["window"]
+    a0, a1 = t["active"]
+    d = int(cfg.diagonal_width)
+    bin_size = int(cfg.bin_size)
+    nrows, ncols = engine.band_shape(cfg, we - ws)
+    part = a0 + d
+    lines = []
+    for i, f1 in enumerate(feats1):
+        c1 = (f1[1] + f1[2] + 1) // 2
+        for f2 in feats2[i:]:
+            if not last_window and f1[1] >= part and f2[1] >= part:
+                continue
+            c2 = (f2[1] + f2[2] + 1) // 2
+            b1r, b2r = (c1 - ws) // bin_size, (c2 - ws) // bin_size
+            cont = band_block(result.band, nrows, ncols, b1r, b2r, block_size)
+            ref = band_block(ref_window_band, nrows, ncols, b1r, b2r, block_size)
+            if cont == 0 and ref == 0:
+                continue
+            if ref == 0:
+                score = 999.0
+            elif cont == 0:
+                score = -999.0
+            else:
+                score = min(max(float(np.log2(cont / ref)), -999.0), 999.0)
+            sig = binomial_test(cont, ref + cont)
+            b1, b2 = c1 // bin_size, c2 // bin_size
+            name = f"{f1[3] or 'none'};{f2[3] or 'none'}"
+            lines.append("\t".join(str(x) for x in (
+                f1[0], b1 * bin_size, (b1 + 1) * bin_size, f2[0], b2 * bin_size, (b2 + 1) * bin_size,
+                name, format(score, ".4G"), f1[4], f2[4], ref, cont, format(sig, ".4G"),
+                t["deletion"][0], t["deletion"][1], t["active_barriers"], len(t["barriers"]),
+                a0, a1, ws, we, t["cell_id"])))
+    return lines

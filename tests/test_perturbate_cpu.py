@@ -75,3 +75,48 @@ def test_oracle_window_spanning_the_chromosome_is_the_plain_cell():
         assert rc == 0
         out.append((band, (st.epochs, st.contacts, st.rng_draws)))
     assert np.array_equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
+
+
+def test_block_sums_extend_edges_and_stay_in_the_band():
+    nrows, ncols = 3, 6
+    band = np.arange(1, nrows * ncols + 1, dtype=np.uint32)  # column j, row r at j * nrows + r
+    for j in range(ncols):
+        for r in range(nrows):
+            if r > j:
+                band[j * nrows + r] = 0
+    get = lambda i, j: perturbate.band_get(band, nrows, ncols, i, j)
+    assert get(2, 4) == band[4 * nrows + 2] and get(4, 2) == get(2, 4) and get(0, 5) == 0
+    # 3x3 block at the corner (0, 0): rows and columns -1 clamp to 0
+    want = sum(get(min(max(i, 0), ncols - 1), min(max(j, 0), ncols - 1)) for i in (-1, 0, 1) for j in (-1, 0, 1))
+    assert perturbate.band_block(band, nrows, ncols, 0, 0, 3) == want
+    assert perturbate.band_block(band, nrows, ncols, 2, 3, 1) == get(2, 3)
+
+
+def test_window_band_and_scores():
+    cfg = genome.parity_config(diagonal_width=20_000, bin_size=5000)
+    nrows, ncols = engine.band_shape(cfg, 100_000)
+    rng = np.random.default_rng(2)
+    full = rng.integers(0, 9, size=nrows * ncols).astype(np.uint32)
+    win = perturbate.window_band_of(cfg, full, nrows, 20_000, 60_000)
+    wr, wc = engine.band_shape(cfg, 40_000)
+    for jr in range(wc):
+        for r in range(min(wr, jr + 1)):
+            assert win[jr * wr + r] == full[(4 + jr) * nrows + r]
+    task = dict(window=(20_000, 60_000), active=(20_000, 40_000), deletion=(30_000, 31_000), cell_id=7,
+                active_barriers=2, barriers=[{}, {}, {}])
+    sim = win.copy()
+    sim[0] += 5
+    res = perturbate.WindowResult(engine.Chromosome("chrW", 100_000), task, sim, None)
+    feats1 = [("chrW", 21_000, 21_001, "a", "+")]
+    feats2 = [("chrW", 24_000, 24_001, "", "-"), ("chrW", 45_000, 45_001, "b", "+")]
+    lines = perturbate.score_window(cfg, res, win, feats1, feats2, block_size=1)
+    rows = [ln.split("\t") for ln in lines]
+    assert all(r[6] in ("a;none", "a;b") for r in rows)
+    for r in rows:
+        ref, cont = int(r[10]), int(r[11])
+        assert ref + cont > 0
+        if ref and cont:
+            assert abs(float(r[7]) - np.log2(cont / ref)) < 1e-3 * max(1.0, abs(np.log2(cont / ref)))
+        assert r[13:] == ["30000", "31000", "2", "3", "20000", "40000", "20000", "60000", "7"]
+    assert perturbate.binomial_test(5, 10) == 1.0
+    assert abs(perturbate.binomial_test(0, 10) - 2 * 0.5 ** 10) < 1e-12
