@@ -1207,13 +1207,55 @@ __device__ bool rank_dir_split(Cell& c, u32 dir, u32 n) {
     }
   }
   __syncwarp();
-  // sort B by key (events are dead: sf is free)
+  // sort B by key (events are dead: sf is free).  When sf has room, the keys are loaded once
+  // and sorted alongside the indices, so the network compares values already in memory.
   u32* Bs = c.sf;
-  for (u32 t = lane; t < kE; t += 32) Bs[t] = B[t];
-  __syncwarp();
-  bitonic_by_key(c, dir, Bs, kE);
   bool full_tie = false;
-  for (u32 t = lane + 1; t < kE; t += 32) full_tie |= rank_key(c, dir, Bs[t - 1]) == rank_key(c, dir, Bs[t]);
+  if (3 * kE + 1 <= n) {
+    // 8-byte aligned start at or after sf + kE (sf itself is only 4-byte aligned when n is odd)
+    const u32 koff = kE + (u32)(((reinterpret_cast<uintptr_t>(c.sf) >> 2) + kE) & 1u);
+    u64* Kb = reinterpret_cast<u64*>(c.sf + koff);
+    for (u32 t = lane; t < kE; t += 32) {
+      const u32 idx = B[t];
+      Bs[t] = idx;
+      Kb[t] = rank_key(c, dir, idx);
+    }
+    __syncwarp();
+    u32 p2 = 1;
+    while (p2 < kE) p2 <<= 1;
+    auto cmpx = [&](u32 i, u32 j) {
+      if (j >= kE) return;
+      const u64 ki = Kb[i], kj = Kb[j];
+      if (ki > kj) {
+        Kb[i] = kj;
+        Kb[j] = ki;
+        const u32 x = Bs[i];
+        Bs[i] = Bs[j];
+        Bs[j] = x;
+      }
+    };
+    for (u32 size = 2; size <= p2; size <<= 1) {
+      const u32 half = size >> 1;
+      for (u32 t = lane; t < p2 / 2; t += 32) {
+        const u32 base = (t / half) * size, off = t % half;
+        cmpx(base + off, base + size - 1 - off);
+      }
+      __syncwarp();
+      for (u32 stride = half >> 1; stride > 0; stride >>= 1) {
+        for (u32 t = lane; t < p2 / 2; t += 32) {
+          const u32 i = 2 * stride * (t / stride) + (t % stride);
+          cmpx(i, i + stride);
+        }
+        __syncwarp();
+      }
+    }
+    for (u32 t = lane + 1; t < kE; t += 32) full_tie |= Kb[t - 1] == Kb[t];
+  } else {
+    for (u32 t = lane; t < kE; t += 32) Bs[t] = B[t];
+    __syncwarp();
+    bitonic_by_key(c, dir, Bs, kE);
+    for (u32 t = lane + 1; t < kE; t += 32) full_tie |= rank_key(c, dir, Bs[t - 1]) == rank_key(c, dir, Bs[t]);
+  }
   const u32* Bf = Bs;
   if (__any_sync(FULL, full_tie)) {
     prof_add(c, PF_RANK_PDQ, 1);
