@@ -261,6 +261,15 @@ int mgpu_upload_window(mgpu_ctx* ctx, const mgpu_chrom* chrom, uint64_t window_s
                        uint64_t window_end, const mgpu_barrier* barriers, uint64_t nbarriers,
                        int* chrom_id);
 
+/* Give one uploaded chromosome (or window) its own configuration, used instead of the
+ * context's for every later launch that simulates it; NULL restores the context's.  The
+ * reference runs one Config per process (simulation.hpp); with this a single
+ * mgpu_simulate_batch launch advances windows of different bin sizes, LEF densities, lifetimes
+ * and speeds, each cell exactly as a context created with that configuration would simulate
+ * it.  The configuration is validated like mgpu_create's and must already be transformed
+ * (mgpu_config_transform). */
+int mgpu_set_chrom_config(mgpu_ctx* ctx, int chrom_id, const mgpu_config* cfg);
+
 /*
  * Simulate `ncells` cells of one chromosome: the drop-in for calling
  * Simulation::simulate_one_cell once per task (scheduler_simulate.cpp:229-256).

@@ -538,6 +538,8 @@ extern "C" uint64_t mgpu_state_digest(uint64_t n, const uint64_t* rev, const uin
 struct ChromEntry {
   mgpu_chrom chrom{};
   uint64_t ws = 0, we = 0;  // simulated window (the whole range unless uploaded as a window)
+  bool own_cfg = false;     // cfg overrides the context's configuration
+  mgpu_config cfg{};
   std::string name;
   DevBarrier* d_bars = nullptr;
   uint2* d_pos_flags = nullptr;  // inside the d_bars allocation
@@ -712,9 +714,24 @@ extern "C" int mgpu_upload_window(mgpu_ctx* ctx, const mgpu_chrom* chrom, uint64
   return MGPU_OK;
 }
 
+extern "C" int mgpu_set_chrom_config(mgpu_ctx* ctx, int chrom_id, const mgpu_config* cfg) {
+  if (!ctx) return fail(MGPU_ERR_INVALID_ARG, "mgpu_set_chrom_config: null context");
+  if (cfg) {
+    const int rc = validate_config(cfg);
+    if (rc) return rc;
+  }
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (chrom_id < 0 || chrom_id >= (int)ctx->chroms.size())
+    return fail(MGPU_ERR_INVALID_ARG, "unknown chromosome handle %d", chrom_id);
+  ChromEntry& e = ctx->chroms[chrom_id];
+  e.own_cfg = cfg != nullptr;
+  if (cfg) e.cfg = *cfg;
+  return MGPU_OK;
+}
+
 static int make_kparams(const mgpu_ctx* ctx, const ChromEntry& ch, uint64_t nlefs, KParams* P,
                         uint64_t budget_override = 0) {
-  const mgpu_config& c = ctx->cfg;
+  const mgpu_config& c = ch.own_cfg ? ch.cfg : ctx->cfg;
   std::memset(P, 0, sizeof(*P));
   if (nlefs == 0) return fail(MGPU_ERR_INVALID_ARG, "num_lefs must be positive");
   if (nlefs >= (1ull << 27)) return fail(MGPU_ERR_UNSUPPORTED, "too many LEFs");

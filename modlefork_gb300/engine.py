@@ -56,6 +56,7 @@ def load(path=LIB_PATH):
         "mgpu_sync": (i32, [C.c_void_p]),
         "mgpu_upload_chrom": (i32, [C.c_void_p, P(abi.Chrom), P(abi.Barrier), u64, P(i32)]),
         "mgpu_upload_window": (i32, [C.c_void_p, P(abi.Chrom), u64, u64, P(abi.Barrier), u64, P(i32)]),
+        "mgpu_set_chrom_config": (i32, [C.c_void_p, i32, P(abi.Config)]),
         "mgpu_simulate_cells": (i32, [C.c_void_p, i32, C.c_void_p, C.c_void_p, u64, u64, u64,
                                       C.c_void_p, C.c_void_p, C.c_void_p]),
         "mgpu_simulate_cells_noalloc": (i32, [C.c_void_p, i32, C.c_void_p, C.c_void_p, u64, u64, u64,
@@ -224,6 +225,12 @@ class Engine:
                                            C.byref(cid)), "mgpu_upload_window")
         self.chroms[cid.value] = chrom
         return cid.value
+
+    def set_chrom_config(self, chrom_id, cfg):
+        """mgpu_set_chrom_config: simulate ``chrom_id`` with its own (transformed) configuration
+        instead of the engine's; None restores the engine's."""
+        _check(self.lib.mgpu_set_chrom_config(self.h, chrom_id, C.byref(cfg) if cfg is not None else None),
+               "mgpu_set_chrom_config")
 
     def simulate_cells(self, chrom_id, seeds, targets, target_epochs, nlefs, band=None,
                        stats=True, ncells=None):

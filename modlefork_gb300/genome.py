@@ -11,6 +11,9 @@ parity and genome-scale workloads:
 * ``genome_24chr``: 24 chromosomes with lengths uniform in [50, 250] Mbp, one barrier per
   50 kb on average at uniform positions, random strands, occupancy ~ Beta(8, 2) written to
   the BED score, 20 LEFs/Mbp, 200 kb lifetime, default speeds (0.8 x bin), 512 cells each.
+* ``batched_windows``: windows of uneven length (log-uniform in [1, 250] Mbp, 4096 of them at
+  full size), each with its own configuration: bin size uniform_int{1..10} kb, LEF density
+  U(5, 40)/Mbp, barrier density U(5, 40)/Mbp, barriers and the rest as ``genome_24chr``.
 
 Barriers are produced as BED records [p, p + 1) (so the reference's midpoint rule
 (start + end + 1) / 2 of genome.cpp:199 puts the barrier at p + 1) in IITree order (sorted by
@@ -83,3 +86,24 @@ def genome_24chr(seed=11, nchroms=24, min_len=50_000_000, max_len=250_000_000, *
         bars = engine.barriers_from_bed(chrom, recs, cfg.barrier_occupied_stp, cfg.barrier_not_occupied_stp)
         out.append((chrom, bars))
     return cfg, out
+
+
+def batched_windows(seed=13, nwindows=4096, min_len=1_000_000, max_len=250_000_000, cells=256, **overrides):
+    """Windows of the batched workload, each a sequence of its own with its own transformed
+    configuration; returns a list of (cfg, chrom, barriers)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(nwindows):
+        L = int(round(float(np.exp(rng.uniform(np.log(min_len), np.log(max_len))))))
+        bin_size = 1000 * int(rng.integers(1, 11))
+        lef_density = float(rng.uniform(5.0, 40.0))
+        bar_density = float(rng.uniform(5.0, 40.0))
+        cfg = genome_config(bin_size=bin_size, number_of_lefs_per_mbp=lef_density, num_cells=cells,
+                            **overrides)
+        chrom = engine.Chromosome(f"win{k + 1}", L)
+        nb = int(round(L / 1e6 * bar_density))
+        occ = rng.beta(8.0, 2.0, size=nb)
+        recs = bed_records(rng, L, nb, occ)
+        bars = engine.barriers_from_bed(chrom, recs, cfg.barrier_occupied_stp, cfg.barrier_not_occupied_stp)
+        out.append((cfg, chrom, bars))
+    return out

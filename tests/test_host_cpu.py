@@ -142,3 +142,21 @@ def test_engine_fails_loudly_without_device(lib):
     with pytest.raises(engine.EngineError) as e:
         engine.Engine(engine.config_transform(engine.config_defaults()))
     assert e.value.code in (abi.MGPU_ERR_NO_DEVICE, abi.MGPU_ERR_CUDA)
+
+
+def test_batched_windows_follow_the_workload_ranges(lib):
+    from modlefork_gb300 import genome
+
+    wins = genome.batched_windows(seed=21, nwindows=400, min_len=1_000_000, max_len=250_000_000, cells=4)
+    sizes = np.array([w[1].size for w in wins], dtype=np.float64)
+    assert sizes.min() >= 1_000_000 and sizes.max() <= 250_000_000
+    # log-uniform: about half the windows below the geometric midpoint (~15.8 Mbp)
+    assert 0.4 < float(np.mean(sizes < np.sqrt(1e6 * 250e6))) < 0.6
+    bins = {int(w[0].bin_size) for w in wins}
+    assert bins == {1000 * k for k in range(1, 11)}
+    dens = np.array([w[0].number_of_lefs_per_mbp for w in wins])
+    assert dens.min() >= 5.0 and dens.max() <= 40.0
+    bden = np.array([len(w[2]) / (w[1].size / 1e6) for w in wins])
+    assert bden.min() > 4.0 and bden.max() < 41.0
+    for cfg, chrom, bars in wins[:5]:
+        assert cfg.num_cells == 4 and np.isclose(cfg.rev_extrusion_speed, 0.8 * cfg.bin_size)
