@@ -46,6 +46,15 @@ namespace mgpu {
 #define MGPU_ITER_LIMIT 100000000ull
 #define FULL 0xFFFFFFFFu
 
+// Items per lane in the chunked sweeps: the per-LEF arrays of large cells live in global
+// memory, where every dependent load waits for L2; a lane that carries MLP independent items
+// through each stage of a sweep keeps MLP loads in flight instead of one.
+#ifndef MGPU_MLP
+#define MGPU_MLP 2
+#endif
+constexpr unsigned MLP = MGPU_MLP;
+
+
 __device__ __forceinline__ u64 rotl64(u64 x, int k) { return (x << k) | (x >> (64 - k)); }
 
 __device__ __forceinline__ u64 xo_next(u64* s) {
@@ -947,25 +956,44 @@ __device__ void barriers_init(Cell& c, u64* s) {
 
 // ExtrusionBarriers::next_state (extrusion_barriers.cpp:145-161): one draw per barrier.
 __device__ void barriers_next(Cell& c, u64* s) {
-  for (u32 base = 0; base < c.nb; base += 32) {
-    rng_ensure(c, s, 32);
-    const u32 i = base + ln();
-    const bool valid = i < c.nb;
-    bool st = (c.bst[base >> 5] >> ln()) & 1u;
-    if (valid) {
-      const u64 u = ring_at(c, c.sc->rpos + ln());
-      const u32 f = bar_flags(c, i);
-      if (!st) {
-        st = !(f & BF_INA_NEVER) && u >= c.bar[i].t_ina;
-      } else {
-        st = !(!(f & BF_ACT_NEVER) && u >= c.bar[i].t_act);
-      }
+  const u32 nwords = (c.nb + 31) / 32;
+  for (u32 base = 0; base < c.nb; base += 32 * MLP) {
+    rng_ensure(c, s, 32 * MLP);
+    const u64 r0 = c.sc->rpos;
+    u32 word[MLP], f[MLP];
+    u64 thr[MLP], u[MLP];
+    bool st[MLP], valid[MLP];
+#pragma unroll
+    for (u32 h = 0; h < MLP; ++h) {
+      const u32 i = base + 32 * h + ln();
+      valid[h] = i < c.nb;
+      const u32 w = (base >> 5) + h;
+      word[h] = w < nwords ? c.bst[w] : 0u;
+      st[h] = (word[h] >> ln()) & 1u;
+      const u32 ic = valid[h] ? i : 0u;
+      f[h] = bar_flags(c, ic);
+      thr[h] = st[h] ? c.bar[ic].t_act : c.bar[ic].t_ina;
+      u[h] = ring_at(c, r0 + 32 * h + ln());
     }
-    const unsigned nm = __ballot_sync(FULL, valid && st);
+    unsigned nm[MLP];
+#pragma unroll
+    for (u32 h = 0; h < MLP; ++h) {
+      bool nst = st[h];
+      if (valid[h]) {
+        if (!st[h]) {
+          nst = !(f[h] & BF_INA_NEVER) && u[h] >= thr[h];
+        } else {
+          nst = !(!(f[h] & BF_ACT_NEVER) && u[h] >= thr[h]);
+        }
+      }
+      nm[h] = __ballot_sync(FULL, valid[h] && nst);
+    }
     __syncwarp();
     if (ln() == 0) {
-      c.bst[base >> 5] = nm;
-      c.sc->rpos += min(32u, c.nb - base);
+#pragma unroll
+      for (u32 h = 0; h < MLP; ++h)
+        if ((base >> 5) + h < nwords) c.bst[(base >> 5) + h] = nm[h];
+      c.sc->rpos = r0 + min(32u * MLP, c.nb - base);
     }
     __syncwarp();
   }
@@ -1371,7 +1399,9 @@ __device__ void gather_ranked(Cell& c, u32 n) {
 // chain s0 = 0, s(j+1) = s(j) + len(s(j)); lane j finds s(j) by binary lifting over the
 // lanes' next-start pointers.  A window serves the normals whose start lies inside it (31 or
 // 32 of them in the common case), in stream order, to the next LEFs in index order.
-__device__ void gen_moves_dir(Cell& c, u64* s, u32* mv, u32 n, double mean, double sd, u64 move_int) {
+// Kept out of line: inlined into the epoch loop it shares the kernel's register allocation,
+// and the batched genome launch took 13 % longer that way.
+__device__ __noinline__ void gen_moves_dir(Cell& c, u64* s, u32* mv, u32 n, double mean, double sd, u64 move_int) {
   if (sd == 0.0) {
     for (u32 i = ln(); i < n; i += 32) mv[i] = c.bep[i] == UNBOUND ? 0u : (u32)move_int;
     __syncwarp();
@@ -1455,13 +1485,35 @@ __device__ bool adjust_rev_fast(Cell& c, const KParams& P, u32 n) {
   i64 carry_u = 0;       // U of element kb + 32
   bool carry_b = false;  // bound flag of element kb + 32
   bool bad = false;
-  for (i64 kb = ((i64)n - 1) / 32 * 32; kb >= 0; kb -= 32) {
+  {
+  // the chunk below is loaded while this one is scanned (the scan writes only tmp)
+  const u32* __restrict__ rr = c.rr;
+  const u32* __restrict__ sr = c.sr;
+  const u32* __restrict__ bep = c.bep;
+  const u32* __restrict__ rm = c.rm;
+  i64 kb = ((i64)n - 1) / 32 * 32;
+  u32 idx_n = 0, sp_n = 0, be_n = UNBOUND, m_n = 0;
+  {
     const i64 k = kb + ln();
     const bool valid = k < (i64)n;
-    const u32 idx = valid ? c.rr[k] : 0;
-    const bool b = valid && c.bep[idx] != UNBOUND;
-    const i64 p = valid ? (i64)c.sr[k] : 0;
-    const i64 t = valid ? p - (i64)c.rm[idx] : 0;
+    idx_n = valid ? rr[k] : 0u;
+    sp_n = valid ? sr[k] : 0u;
+    be_n = valid ? bep[idx_n] : UNBOUND;
+    m_n = valid ? rm[idx_n] : 0u;
+  }
+  for (; kb >= 0; kb -= 32) {
+    const i64 k = kb + ln();
+    const bool valid = k < (i64)n;
+    const bool b = valid && be_n != UNBOUND;
+    const i64 p = valid ? (i64)sp_n : 0;
+    const i64 t = valid ? p - (i64)m_n : 0;
+    if (kb >= 32) {
+      const i64 k2 = kb - 32 + ln();
+      idx_n = rr[k2];
+      sp_n = sr[k2];
+      be_n = bep[idx_n];
+      m_n = rm[idx_n];
+    }
     bool b_next = __shfl_down_sync(FULL, b, 1);
     if (ln() == 31) b_next = carry_b;
     const bool link_next = valid && k + 1 < (i64)n && b && b_next && t > start;
@@ -1485,6 +1537,7 @@ __device__ bool adjust_rev_fast(Cell& c, const KParams& P, u32 n) {
     carry_u = __shfl_sync(FULL, v, 0);
     carry_b = __shfl_sync(FULL, b, 0);
   }
+  }
   if (__any_sync(FULL, bad)) return false;
   __syncwarp();
 #pragma unroll 4
@@ -1501,13 +1554,34 @@ __device__ bool adjust_fwd_fast(Cell& c, const KParams& P, u32 n) {
   i64 carry_v = 0;       // V of element kb - 1
   bool carry_b = false;  // bound flag of element kb - 1
   bool bad = false;
+  {
+  // the next chunk is loaded while this one is scanned (the scan writes only tmp)
+  const u32* __restrict__ fr = c.fr;
+  const u32* __restrict__ sf = c.sf;
+  const u32* __restrict__ bep = c.bep;
+  const u32* __restrict__ fm = c.fm;
+  u32 idx_n = 0, sp_n = 0, be_n = UNBOUND, m_n = 0;
+  if (ln() < n) {
+    idx_n = fr[ln()];
+    sp_n = sf[ln()];
+    be_n = bep[idx_n];
+    m_n = fm[idx_n];
+  }
   for (u32 kb = 0; kb < n; kb += 32) {
     const i64 k = (i64)kb + ln();
     const bool valid = k < (i64)n;
-    const u32 idx = valid ? c.fr[k] : 0;
-    const bool b = valid && c.bep[idx] != UNBOUND;
-    const i64 p = valid ? (i64)c.sf[k] : 0;
-    const i64 t = valid ? p + (i64)c.fm[idx] : 0;
+    const bool b = valid && be_n != UNBOUND;
+    const i64 p = valid ? (i64)sp_n : 0;
+    const i64 t = valid ? p + (i64)m_n : 0;
+    {
+      const u32 k2 = kb + 32 + ln();
+      if (k2 < n) {
+        idx_n = fr[k2];
+        sp_n = sf[k2];
+        be_n = bep[idx_n];
+        m_n = fm[idx_n];
+      }
+    }
     bool b_prev = __shfl_up_sync(FULL, b, 1);
     if (ln() == 0) b_prev = carry_b;
     const bool link_prev = valid && k > 0 && b && b_prev && t <= endm1;
@@ -1530,6 +1604,7 @@ __device__ bool adjust_fwd_fast(Cell& c, const KParams& P, u32 n) {
     if (valid) out[k] = (u32)(T - p);
     carry_v = __shfl_sync(FULL, v, 31);
     carry_b = __shfl_sync(FULL, b, 31);
+  }
   }
   if (__any_sync(FULL, bad)) return false;
   __syncwarp();
@@ -1657,6 +1732,31 @@ __device__ __forceinline__ bool trial_outcome(const Trial& t, u64 u) {
   return u <= t.thr;
 }
 
+// ranked_lower_bound of MLP queries at once: the bucket loads and the scans of all queries are
+// issued together.
+__device__ __forceinline__ void ranked_lower_bounds(const BucketIndex& ix, const u32* x, u32* out) {
+  if (!ix.T) {
+#pragma unroll
+    for (u32 h = 0; h < MLP; ++h) out[h] = ranked_lower_bound(ix, x[h]);
+    return;
+  }
+#pragma unroll
+  for (u32 h = 0; h < MLP; ++h) {
+    const u32 b = x[h] <= ix.start ? 0u : min((x[h] - ix.start) >> ix.shift, ix.nbk);
+    out[h] = x[h] <= ix.start ? 0u : ix.T[b];
+  }
+  for (;;) {
+    bool more = false;
+#pragma unroll
+    for (u32 h = 0; h < MLP; ++h) {
+      const bool a = out[h] < ix.n && ix.key[out[h]] < x[h];
+      out[h] += a ? 1u : 0u;
+      more |= a;
+    }
+    if (!more) break;
+  }
+}
+
 // detect_lef_bar_collisions (simulation_detect_collisions.cpp:128-252), warp-parallel.  For
 // an occupied barrier the reference's sweep tests the first rev unit (in rank order, from
 // index max(n5 - 1, 0)) strictly downstream of it and the last fwd unit strictly upstream of
@@ -1664,80 +1764,88 @@ __device__ __forceinline__ bool trial_outcome(const Trial& t, u64 u) {
 // Trials draw in barrier order (ascending for rev units, descending for fwd units); a unit
 // hit by several barriers keeps the last successful one in that order.
 __device__ void detect_lef_bar_fast(Cell& c, u64* s, const KParams& P, u32 n, u64 n5, u64 n3) {
-  const u32 j0 = (u32)min(n5, n5 - 1);
-  const BucketIndex ixr = build_bucket_index(c.sr, n, (u32)P.start, (u32)P.end, c.tmp);
-  for (u32 base = 0; base < c.nb; base += 32) {
-    rng_ensure(c, s, 32);
-    const u32 i = base + ln();
-    bool cand = false, drawn = false;
-    u32 unit = 0;
-    if (i < c.nb && bar_active(c, i)) {
-      const u32 bpos = bar_pos(c, i);
-      const u32 lo = max(j0, ranked_lower_bound(ixr, bpos + 1));  // first k >= j0 with sr[k] > bpos
-      if (lo < n) {
-        unit = c.rr[lo];
-        if (c.bep[unit] != UNBOUND) {
-          const u64 delta = (u64)c.sr[lo] - bpos;
-          const Trial& tr = P.lef_bar[(bar_flags(c, i) & BF_DIR_MASK) == MGPU_DIR_REV ? 0 : 1];
-          if (delta > 0 && delta <= c.rm[unit]) {
+  const u32* __restrict__ rr = c.rr;
+  const u32* __restrict__ fr = c.fr;
+  const u32* __restrict__ sr = c.sr;
+  const u32* __restrict__ sf = c.sf;
+  const u32* __restrict__ bep = c.bep;
+  const u32* __restrict__ rm = c.rm;
+  const u32* __restrict__ fm = c.fm;
+  for (u32 dir = 0; dir < 2; ++dir) {
+    // rev: first k >= j0 with sr[k] > bpos; fwd: last k <= jtop with sf[k] < bpos
+    const u32 j0 = (u32)min(n5, n5 - 1);
+    const u32 jtop = (u32)(n - min(n3, n3 - 1)) - 1;
+    const BucketIndex ix = build_bucket_index(dir ? sf : sr, n, (u32)P.start, (u32)P.end, c.tmp);
+    const u32 nchunks = (c.nb + 32 * MLP - 1) / (32 * MLP);
+    for (u32 ch = 0; ch < nchunks; ++ch) {
+      rng_ensure(c, s, 32 * MLP);
+      u32 bi[MLP], bpos[MLP], x[MLP], lo[MLP], k[MLP], unit[MLP], kpos[MLP], be[MLP], mv[MLP];
+      bool act[MLP];
+      int ti[MLP];
+#pragma unroll
+      for (u32 h = 0; h < MLP; ++h) {
+        const i64 i = dir ? (i64)c.nb - 1 - (i64)(ch * 32 * MLP + 32 * h + ln()) : (i64)(ch * 32 * MLP + 32 * h + ln());
+        act[h] = i >= 0 && i < (i64)c.nb && bar_active(c, (u32)i);
+        bi[h] = act[h] ? (u32)i : 0u;
+        const uint2 pf = act[h] ? __ldg(&c.bpf[bi[h]]) : make_uint2(0u, 0u);
+        bpos[h] = pf.x;
+        const u32 bdir = pf.y & BF_DIR_MASK;
+        ti[h] = dir ? (bdir == MGPU_DIR_FWD ? 0 : 1) : (bdir == MGPU_DIR_REV ? 0 : 1);
+        x[h] = act[h] ? (dir ? pf.x : pf.x + 1) : 0u;
+      }
+      ranked_lower_bounds(ix, x, lo);
+#pragma unroll
+      for (u32 h = 0; h < MLP; ++h) {
+        bool ok;
+        if (dir == 0) {
+          lo[h] = max(j0, lo[h]);
+          ok = lo[h] < n;
+          k[h] = ok ? lo[h] : 0u;
+        } else {
+          lo[h] = min(jtop + 1, lo[h]);
+          ok = lo[h] > 0;
+          k[h] = ok ? lo[h] - 1 : 0u;
+        }
+        act[h] = act[h] && ok;
+        unit[h] = dir ? fr[k[h]] : rr[k[h]];
+        kpos[h] = dir ? sf[k[h]] : sr[k[h]];
+      }
+#pragma unroll
+      for (u32 h = 0; h < MLP; ++h) {
+        be[h] = bep[unit[h]];
+        mv[h] = dir ? fm[unit[h]] : rm[unit[h]];
+      }
+      u32 used = 0;
+#pragma unroll
+      for (u32 h = 0; h < MLP; ++h) {
+        bool cand = false, drawn = false;
+        if (act[h] && be[h] != UNBOUND) {
+          const u64 delta = dir ? (u64)bpos[h] - kpos[h] : (u64)kpos[h] - bpos[h];
+          if (delta > 0 && delta <= mv[h]) {
             cand = true;
-            drawn = trial_needs_draw(tr);
+            drawn = trial_needs_draw(P.lef_bar[ti[h]]);
           }
         }
-      }
-    }
-    const unsigned dm = __ballot_sync(FULL, drawn);
-    bool hit = false;
-    if (cand) {
-      const Trial& tr = P.lef_bar[(bar_flags(c, i) & BF_DIR_MASK) == MGPU_DIR_REV ? 0 : 1];
-      const u64 u = drawn ? ring_at(c, c.sc->rpos + __popc(dm & lanemask_lt())) : 0;
-      hit = trial_outcome(tr, u);
-    }
-    // the highest barrier index wins among this chunk's hits on the same unit
-    const unsigned hm = __ballot_sync(FULL, hit);
-    const unsigned same = __match_any_sync(FULL, hit ? unit : 0xFFFFFFFFu);
-    if (hit && (31 - __clz(same & hm)) == (int)ln()) c.rc[unit] = cw_make(i, EV_COLLISION | EV_LEF_BAR);
-    __syncwarp();
-    if (ln() == 0) c.sc->rpos += __popc(dm);
-    __syncwarp();
-  }
-  const u32 jtop = (u32)(n - min(n3, n3 - 1)) - 1;  // last fwd rank index searched
-  const BucketIndex ixf = build_bucket_index(c.sf, n, (u32)P.start, (u32)P.end, c.tmp);
-  for (i64 top = (i64)c.nb - 1; top >= 0; top -= 32) {
-    rng_ensure(c, s, 32);
-    const i64 ii = top - (i64)ln();
-    bool cand = false, drawn = false;
-    u32 unit = 0;
-    if (ii >= 0 && bar_active(c, (u32)ii)) {
-      const u32 bpos = bar_pos(c, ii);
-      const u32 lo = min(jtop + 1, ranked_lower_bound(ixf, bpos));  // first k <= jtop with sf[k] >= bpos
-      if (lo > 0) {
-        const u32 k = lo - 1;
-        unit = c.fr[k];
-        if (c.bep[unit] != UNBOUND) {
-          const u64 delta = (u64)bpos - c.sf[k];
-          const Trial& tr = P.lef_bar[(bar_flags(c, ii) & BF_DIR_MASK) == MGPU_DIR_FWD ? 0 : 1];
-          if (delta > 0 && delta <= c.fm[unit]) {
-            cand = true;
-            drawn = trial_needs_draw(tr);
-          }
+        const unsigned dm = __ballot_sync(FULL, drawn);
+        bool hit = false;
+        if (cand) {
+          const u64 u = drawn ? ring_at(c, c.sc->rpos + used + __popc(dm & lanemask_lt())) : 0;
+          hit = trial_outcome(P.lef_bar[ti[h]], u);
         }
+        used += __popc(dm);
+        // within an item the highest lane is the last barrier in sweep order; later items
+        // overwrite earlier ones
+        const unsigned hm = __ballot_sync(FULL, hit);
+        const unsigned same = __match_any_sync(FULL, hit ? unit[h] : 0xFFFFFFFFu);
+        if (hit && (31 - __clz(same & hm)) == (int)ln()) {
+          const u32 w = cw_make(bi[h], EV_COLLISION | EV_LEF_BAR);
+          if (dir) c.fc[unit[h]] = w; else c.rc[unit[h]] = w;
+        }
+        __syncwarp();
       }
+      if (ln() == 0) c.sc->rpos += used;
+      __syncwarp();
     }
-    const unsigned dm = __ballot_sync(FULL, drawn);
-    bool hit = false;
-    if (cand) {
-      const Trial& tr = P.lef_bar[(bar_flags(c, ii) & BF_DIR_MASK) == MGPU_DIR_FWD ? 0 : 1];
-      const u64 u = drawn ? ring_at(c, c.sc->rpos + __popc(dm & lanemask_lt())) : 0;
-      hit = trial_outcome(tr, u);
-    }
-    // loop order is descending barrier index: the last hit on a unit is the highest lane
-    const unsigned hm = __ballot_sync(FULL, hit);
-    const unsigned same = __match_any_sync(FULL, hit ? unit : 0xFFFFFFFFu);
-    if (hit && (31 - __clz(same & hm)) == (int)ln()) c.fc[unit] = cw_make((u32)ii, EV_COLLISION | EV_LEF_BAR);
-    __syncwarp();
-    if (ln() == 0) c.sc->rpos += __popc(dm);
-    __syncwarp();
   }
 }
 
@@ -1987,28 +2095,47 @@ __device__ void secondary_dir_fast(Cell& c, u64* s, const KParams& P, u32 dir, u
 // adjacent in rank order (the unit before a rev candidate, after a fwd candidate, is stalled),
 // so each is an independent swap of two neighbours.
 __device__ bool fix_secondary_fast(Cell& c, const KParams& P, u32 n, u64 n5, u64 n3) {
-  const u64 k0 = max((u64)1, n5);
+  const u32 k0 = (u32)max((u64)1, n5);
+  const u32 naf = (u32)(n - min(n3, n3 - 1));
+  u32* list = c.tmp;
+  u32 nr = 0, nf = 0;
   bool adj = false;
-  for (u64 i = k0 + ln(); i < n; i += 32) {
-    if (cw_avoided_as(c.rc[c.rr[i]], EV_SECONDARY) && i + 1 < n &&
-        cw_avoided_as(c.rc[c.rr[i + 1]], EV_SECONDARY))
-      adj = true;
+  for (u32 dir = 0; dir < 2; ++dir) {
+    const u32* __restrict__ R = dir ? c.fr : c.rr;
+    const u32* __restrict__ W = dir ? c.fc : c.rc;
+    // candidate ranks: rev [k0, n), fwd [0, naf - 1)
+    const u32 lo = dir ? 0u : k0, hi = dir ? (naf > 0 ? naf - 1 : 0u) : n;
+    bool prev = false;  // avoided flag of the rank before the item
+    u32& cnt = dir ? nf : nr;
+    for (u32 base = lo; base < hi; base += 32 * MLP) {
+      u32 idx[MLP], w[MLP];
+#pragma unroll
+      for (u32 h = 0; h < MLP; ++h) {
+        const u32 k = base + 32 * h + ln();
+        idx[h] = k < hi ? R[k] : 0u;
+      }
+#pragma unroll
+      for (u32 h = 0; h < MLP; ++h) w[h] = W[idx[h]];
+#pragma unroll
+      for (u32 h = 0; h < MLP; ++h) {
+        const u32 k = base + 32 * h + ln();
+        const bool av = k < hi && cw_avoided_as(w[h], EV_SECONDARY);
+        bool before = __shfl_up_sync(FULL, av, 1);
+        if (ln() == 0) before = prev;
+        if (av && before) adj = true;
+        const unsigned m = __ballot_sync(FULL, av);
+        const u32 slot = (dir ? nr + nf : nr) + __popc(m & lanemask_lt());
+        if (av && slot < n) list[slot] = k;
+        cnt += __popc(m);
+        prev = __shfl_sync(FULL, av, 31);
+      }
+    }
   }
-  const u64 naf = n - min(n3, n3 - 1);
-  for (u64 i = ln(); i + 1 < naf; i += 32) {
-    if (cw_avoided_as(c.fc[c.fr[i]], EV_SECONDARY) && i + 2 < naf &&
-        cw_avoided_as(c.fc[c.fr[i + 1]], EV_SECONDARY))
-      adj = true;
-  }
-  if (__any_sync(FULL, adj)) return false;
+  if (__any_sync(FULL, adj) || nr + nf > n) return false;
   __syncwarp();
-  for (u64 i = k0 + ln(); i < n; i += 32) {
-    if (cw_avoided_as(c.rc[c.rr[i]], EV_SECONDARY)) fix_rev_at(c, P.start, i);
-  }
+  for (u32 t = ln(); t < nr; t += 32) fix_rev_at(c, P.start, list[t]);
   __syncwarp();
-  for (u64 i = ln(); i + 1 < naf; i += 32) {
-    if (cw_avoided_as(c.fc[c.fr[i]], EV_SECONDARY)) fix_fwd_at(c, P.end, i);
-  }
+  for (u32 t = ln(); t < nf; t += 32) fix_fwd_at(c, P.end, list[nr + t]);
   __syncwarp();
   return true;
 }
@@ -2092,30 +2219,49 @@ __device__ void extrude(Cell& c, u32 n) {
 // release_lefs (simulation.cpp:544-592): one draw per bound LEF with p > 0.
 __device__ u32 release_lefs(Cell& c, u64* s, const KParams& P, u32 n, bool completed) {
   u32 released = 0;
-  for (u32 base = 0; base < n; base += 32) {
-    rng_ensure(c, s, 32);
-    const u32 i = base + ln();
-    const bool bound = i < n && c.bep[i] != UNBOUND;
-    Trial tr{0, 0, 0};
-    if (bound) {
-      const u32 r = c.rc[i], f = c.fc[i];
-      u32 nh = 0;
-      if (cw_occurred_as(r, EV_LEF_BAR) && (bar_flags(c, cw_idx(r)) & BF_DIR_MASK) == MGPU_DIR_REV) ++nh;
-      if (cw_occurred_as(f, EV_LEF_BAR) && (bar_flags(c, cw_idx(f)) & BF_DIR_MASK) == MGPU_DIR_FWD) ++nh;
-      tr = P.release[completed ? 1 : 0][nh];
+  for (u32 base = 0; base < n; base += 32 * MLP) {
+    rng_ensure(c, s, 32 * MLP);
+    u32 r[MLP], f[MLP], be[MLP], fr_[MLP], ff[MLP];
+#pragma unroll
+    for (u32 h = 0; h < MLP; ++h) {
+      const u32 i = base + 32 * h + ln();
+      const u32 ic = i < n ? i : 0u;
+      be[h] = i < n ? c.bep[ic] : UNBOUND;
+      r[h] = c.rc[ic];
+      f[h] = c.fc[ic];
     }
-    const bool need = bound && tr.draws;
-    const unsigned m = __ballot_sync(FULL, need);
-    const u32 off = __popc(m & lanemask_lt());
-    const bool rel = need && ring_at(c, c.sc->rpos + off) <= tr.thr;
-    if (rel) {
-      c.rev[i] = UNBOUND;
-      c.fwd[i] = UNBOUND;
-      c.bep[i] = UNBOUND;
+#pragma unroll
+    for (u32 h = 0; h < MLP; ++h) {
+      const bool rb = be[h] != UNBOUND && cw_occurred_as(r[h], EV_LEF_BAR);
+      const bool fb = be[h] != UNBOUND && cw_occurred_as(f[h], EV_LEF_BAR);
+      fr_[h] = rb ? bar_flags(c, cw_idx(r[h])) : 0u;
+      ff[h] = fb ? bar_flags(c, cw_idx(f[h])) : 0u;
     }
-    released += __popc(__ballot_sync(FULL, rel));
+    u32 used = 0;
+#pragma unroll
+    for (u32 h = 0; h < MLP; ++h) {
+      const u32 i = base + 32 * h + ln();
+      const bool bound = be[h] != UNBOUND;
+      Trial tr{0, 0, 0};
+      if (bound) {
+        u32 nh = 0;
+        if (cw_occurred_as(r[h], EV_LEF_BAR) && (fr_[h] & BF_DIR_MASK) == MGPU_DIR_REV) ++nh;
+        if (cw_occurred_as(f[h], EV_LEF_BAR) && (ff[h] & BF_DIR_MASK) == MGPU_DIR_FWD) ++nh;
+        tr = P.release[completed ? 1 : 0][nh];
+      }
+      const bool need = bound && tr.draws;
+      const unsigned m = __ballot_sync(FULL, need);
+      const bool rel = need && ring_at(c, c.sc->rpos + used + __popc(m & lanemask_lt())) <= tr.thr;
+      used += __popc(m);
+      if (rel) {
+        c.rev[i] = UNBOUND;
+        c.fwd[i] = UNBOUND;
+        c.bep[i] = UNBOUND;
+      }
+      released += __popc(__ballot_sync(FULL, rel));
+    }
     __syncwarp();
-    if (ln() == 0) c.sc->rpos += __popc(m);
+    if (ln() == 0) c.sc->rpos += used;
     __syncwarp();
   }
   return released;
@@ -3037,6 +3183,7 @@ u64 resident_cells(const KParams& P, u64 ncells) {
     cudaGetLastError();
     return 0;
   }
+  if (max_per_sm && per_sm > (int)max_per_sm) per_sm = (int)max_per_sm;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

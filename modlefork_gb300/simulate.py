@@ -208,6 +208,8 @@ def _main(argv=None):
     ap = argparse.ArgumentParser(description=_main.__doc__)
     ap.add_argument("--workload", choices=["parity", "genome"], default="genome")
     ap.add_argument("--chrom", type=int, action="append", help="chromosome index (repeatable)")
+    ap.add_argument("--chroms", type=int, default=24, help="chromosomes of the generated genome workload")
+    ap.add_argument("--contact-density", type=float, default=None, help="target contact density")
     ap.add_argument("--cells", type=int, default=None)
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--workers", type=int, default=1, help="concurrent chromosome launches")
@@ -217,7 +219,8 @@ def _main(argv=None):
     ap.add_argument("--lef-occupancy", default=None, help="track the 1D LEF occupancy, write it as bedGraph")
     ap.add_argument("--model-state", default=None, help="log the per-epoch model state as TSV")
     args = ap.parse_args(argv)
-    cfg, g = gen.parity_10mbp() if args.workload == "parity" else gen.genome_24chr()
+    ov = {} if args.contact_density is None else {"target_contact_density": args.contact_density}
+    cfg, g = gen.parity_10mbp(**ov) if args.workload == "parity" else gen.genome_24chr(nchroms=args.chroms, **ov)
     if args.chrom:
         g = [g[i] for i in args.chrom]
     if args.cells is not None:
