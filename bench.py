@@ -128,10 +128,10 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def dram_traffic_per_launch(lef_epochs_per_launch):
-    """DRAM bytes per launch of the simulation kernel, from the committed ncu capture's bytes per
+def dram_traffic_per_launch(lef_epochs_per_launch, kernel="simulate_kernel"):
+    """DRAM bytes per launch of a simulation kernel, from the committed ncu capture's bytes per
     LEF-epoch (one launch of the same kernel and layout) scaled to this run's launches."""
-    path = os.path.join(ROOT, "profiles", "simulate_kernel_traffic.json")
+    path = os.path.join(ROOT, "profiles", f"{kernel}_traffic.json")
     if os.path.exists(path):
         d = json.load(open(path))
         return d["bytes_per_lef_epoch"] * lef_epochs_per_launch, d
@@ -419,6 +419,10 @@ def run_ours(args):
         torch.cuda.synchronize()
         bms = bev0.elapsed_time(bev1)
         ble = sum(x.lef_epochs for x in bst)
+        bbytes, off = 0, 0
+        for t in tasks:
+            bbytes += algorithmic_bytes(bst[off:off + len(t["seeds"])], len(t["bars"]))
+            off += len(t["seeds"])
         hb = {w0["cids"][k]: np.zeros(t["nrows"] * t["ncols"], dtype=np.uint32) for k, t in enumerate(tasks)}
         log("batched end to end")
         t0 = time.perf_counter()
@@ -436,6 +440,16 @@ def run_ours(args):
     peak, peak_kind = measured_peak()
     achieved = agg["bytes"] / (ms / 1e3) / 1e9
     traffic, _ = dram_traffic_per_launch(agg["lef_epochs"] / max(1, agg["launches"]))
+    if batched is not None:
+        bach = bbytes / (batched["ms"] / 1e3) / 1e9
+        btraffic, _ = dram_traffic_per_launch(ble, "simulate_batch_kernel")
+        batched["roofline"] = {
+            "bound": "hbm", "achieved": bach, "peak": peak, "unit": "GB/s", "frac": bach / peak,
+            "traffic": btraffic, "peak_source": f"{peak_kind} hbm_gbs", "kernel": "simulate_batch_kernel",
+            "traffic_note": "DRAM bytes of the launch: ncu bytes per LEF-epoch of a one-wave batched "
+                            "launch (profiles/simulate_batch_kernel_traffic.json) x this launch's "
+                            "LEF-epochs; above the algorithmic bytes because the resident cells' arrays "
+                            "exceed L2"}
     timed = sorted({(i * wave + j) % len(tasks) for i in range(args.steps) for j in range(wave)})
     line = {
         "metric": "LEF-epochs/s", "value": agg["lef_epochs"] / (ms / 1e3), "unit": "LEF-epochs/s",
@@ -461,9 +475,10 @@ def run_ours(args):
                      "bytes_model": "24*LEF_epochs + 6*barriers*epochs + 8*contacts, summed over the "
                                     "launches of the timed region / region time (launches overlap)",
                      "traffic_note": "DRAM bytes per launch: ncu bytes per LEF-epoch of one launch "
-                                     "(profiles/simulate_kernel_traffic.json) x this run's LEF-epochs per "
-                                     "launch; far below the algorithmic bytes because the cells' state "
-                                     "stays on chip and in L2"},
+                                     "run alone (profiles/simulate_kernel_traffic.json; ncu serialises "
+                                     "launches) x this run's LEF-epochs per launch; alone, a launch's "
+                                     "cells stay on chip and in L2, while 24 concurrent launches fill "
+                                     "every SM and spill L2 as the batched launch does"},
         "e2e": e2e, "clocks": clk, "batched": batched,
     }
     if not args.no_cpu_baseline:
