@@ -392,7 +392,7 @@ int mgpu_simulate_cells_ex(mgpu_ctx* ctx, int chrom_id, const uint64_t* cell_see
  * stats[i] is task i's outcome (may be NULL).  Results equal one mgpu_simulate_cells call per
  * chromosome.  A shared-memory budget set with mgpu_set_debug_flags applies to every cell;
  * without one, large batches use 16 KiB per cell and a 60 % shared-memory carveout, so that
- * eight cells share an SM and keep a large L1 for their arrays in global slots.
+ * nine cells share an SM and keep an 88 KB L1 for their arrays in global slots.
  */
 typedef struct mgpu_batch_task {
   uint64_t seed;

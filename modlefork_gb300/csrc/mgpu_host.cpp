@@ -1096,8 +1096,8 @@ extern "C" int mgpu_simulate_batch(mgpu_ctx* ctx, const mgpu_batch_task* tasks, 
   }
   int dev_sms = 0;
   cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
-  // Large batches: 16 KiB per cell and a 60 % shared-memory carveout, so that eight cells share
-  // an SM and the per-LEF arrays that live in global slots keep a large L1 (measured best on the
+  // Large batches: 16 KiB per cell and a 60 % shared-memory carveout, so that nine cells share
+  // an SM and the per-LEF arrays that live in global slots keep an 88 KB L1 (measured best on the
   // genome workload).
   const bool large = ntasks >= 8ull * (uint64_t)dev_sms;
   const uint64_t budget = ctx->smem_budget ? ctx->smem_budget : (large ? 16384ull : 0ull);
