@@ -234,7 +234,7 @@ int mgpu_last_kernel_ms(mgpu_ctx* ctx, double* ms);
  * collects the per-step cycle counters of mgpu_last_profile;
  * smem_budget caps the shared memory one cell may use (0 = device limit), placing the
  * remaining per-LEF arrays in global scratch.  Flags bits 8-15 give the shared-memory carveout
- * preference in percent and bits 16-23 cap the cells per SM (0 = the driver's default and the
+ * preference in percent and bits 16-23 cap the cells per SM (0 = the CUDA driver's default and the
  * occupancy limit). */
 int mgpu_set_debug_flags(mgpu_ctx* ctx, uint32_t flags, uint64_t smem_budget);
 

@@ -3228,7 +3228,7 @@ u64 resident_batch_cells(u32 smem_bytes, u64 ntasks, u32 carveout_pct, u32 max_p
     cudaGetLastError();
     return 0;
   }
-  // shared memory / L1 split preference (a tuning switch; -1 lets the driver choose)
+  // shared memory / L1 split preference (a tuning switch; -1 lets the CUDA driver choose)
   cudaFuncSetAttribute(simulate_batch_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                        carveout_pct ? (int)carveout_pct : -1);
   cudaGetLastError();
