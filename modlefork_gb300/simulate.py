@@ -148,6 +148,29 @@ def write_lef_occupancy(path, cfg, results):
                 f.write(f"{r.chrom.name}\t{s0}\t{min(s0 + bin_size, r.chrom.size)}\t{v!r}\n")
 
 
+def occupancy_values(occupancy):
+    """The values Simulation::write_1d_lef_occupancy_to_disk writes (simulation.cpp:245-255):
+    each counter divided by the chromosome's largest, in double, then rounded to float32 (an
+    all-zero track gives NaN, as 0.0 / 0.0 does there)."""
+    occ = np.asarray(occupancy, dtype=np.float64)
+    mx = float(occ.max()) if occ.size else 0.0
+    with np.errstate(invalid="ignore", divide="ignore"):
+        return (occ / mx).astype(np.float32)
+
+
+def write_lef_occupancy_bigwig(path, cfg, results, chroms):
+    """The 1D LEF occupancy track as the reference's bigWig: every chromosome of `chroms`
+    (Chromosome objects, the genome's list) in the chromosome tree, and for each result with a
+    track one fixed-step run of span = step = bin size from the chromosome's start
+    (io::bigwig::Writer::write_range, bigwig_impl.hpp:72-97)."""
+    from . import bigwig
+
+    bin_size = int(cfg.bin_size)
+    tracks = [bigwig.Track(r.chrom.name, r.chrom.start, bin_size, bin_size, occupancy_values(r.occupancy))
+              for r in results if r.occupancy is not None]
+    bigwig.write_bigwig(path, [(c.name, int(c.size)) for c in chroms], tracks)
+
+
 def write_model_state(path, results):
     """Model-state log with the columns of Simulation::dump_stats (simulation.cpp:1166-1224):
     task, epoch, cell, chrom, burn-in, effective barrier occupancy, LEFs, stalled rev / fwd /
@@ -216,7 +239,8 @@ def _main(argv=None):
     ap.add_argument("--batched", action="store_true", help="all chromosomes in one batched launch")
     ap.add_argument("--smem-budget", type=int, default=None, help="shared memory per cell (bytes)")
     ap.add_argument("--pixels", default=None, help="write the pixel table (bin1_id, bin2_id, count) as TSV")
-    ap.add_argument("--lef-occupancy", default=None, help="track the 1D LEF occupancy, write it as bedGraph")
+    ap.add_argument("--lef-occupancy", default=None,
+                    help="track the 1D LEF occupancy, write it as bigWig (.bw, .bigwig) or bedGraph")
     ap.add_argument("--model-state", default=None, help="log the per-epoch model state as TSV")
     args = ap.parse_args(argv)
     ov = {} if args.contact_density is None else {"target_contact_density": args.contact_density}
@@ -240,7 +264,10 @@ def _main(argv=None):
             for a, b, c in zip(b1.tolist(), b2.tolist(), cnt.tolist()):
                 f.write(f"{a}\t{b}\t{c}\n")
     if args.lef_occupancy:
-        write_lef_occupancy(args.lef_occupancy, cfg, res)
+        if args.lef_occupancy.lower().endswith((".bw", ".bigwig")):
+            write_lef_occupancy_bigwig(args.lef_occupancy, cfg, res, [c for c, _ in g])
+        else:
+            write_lef_occupancy(args.lef_occupancy, cfg, res)
     if args.model_state:
         write_model_state(args.model_state, res)
     le = sum(r.lef_epochs for r in res)
