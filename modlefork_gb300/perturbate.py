@@ -152,6 +152,30 @@ def band_block(band, nrows, ncols, row, col, block_size):
     return tot
 
 
+def band_blocks(band, nrows, ncols, rows, cols, block_size):
+    """band_block for many (row, col) centres at once (equal results): the block's indices are
+    clamped to the matrix, mirrored into the upper triangle and read from the band, 0 outside
+    it.  Centres are processed in chunks to bound the temporary arrays."""
+    band = np.asarray(band)
+    rows = np.asarray(rows, dtype=np.int64)
+    cols = np.asarray(cols, dtype=np.int64)
+    out = np.zeros(rows.size, dtype=np.int64)
+    h = block_size // 2 if block_size > 1 else 0
+    off = np.arange(block_size, dtype=np.int64) - h
+    step = max(1, (1 << 22) // max(1, block_size * block_size))
+    for k0 in range(0, rows.size, step):
+        r = rows[k0:k0 + step]
+        c = cols[k0:k0 + step]
+        ii = np.clip(r[:, None, None] + off[None, :, None], 0, ncols - 1)
+        jj = np.clip(c[:, None, None] + off[None, None, :], 0, ncols - 1)
+        lo, hi = np.minimum(ii, jj), np.maximum(ii, jj)
+        d = hi - lo
+        inside = d < nrows
+        vals = np.where(inside, band[np.where(inside, hi * nrows + d, 0)], 0).astype(np.int64)
+        out[k0:k0 + step] = vals.sum(axis=(1, 2))
+    return out
+
+
 def window_band_of(cfg, band, nrows_full, window_start, window_end):
     """The reference run's contacts (a chromosome band with ``nrows_full`` rows) restricted to a
     window, in the window's own band layout (read_reference_contacts,
@@ -190,30 +214,36 @@ def score_window(cfg, result, ref_window_band, feats1, feats2, block_size=9, las
     bin_size = int(cfg.bin_size)
     nrows, ncols = engine.band_shape(cfg, we - ws)
     part = a0 + d
-    lines = []
+    pairs = []
     for i, f1 in enumerate(feats1):
-        c1 = (f1[1] + f1[2] + 1) // 2
         for f2 in feats2[i:]:
             if not last_window and f1[1] >= part and f2[1] >= part:
                 continue
-            c2 = (f2[1] + f2[2] + 1) // 2
-            b1r, b2r = (c1 - ws) // bin_size, (c2 - ws) // bin_size
-            cont = band_block(result.band, nrows, ncols, b1r, b2r, block_size)
-            ref = band_block(ref_window_band, nrows, ncols, b1r, b2r, block_size)
-            if cont == 0 and ref == 0:
-                continue
-            if ref == 0:
-                score = 999.0
-            elif cont == 0:
-                score = -999.0
-            else:
-                score = min(max(float(np.log2(cont / ref)), -999.0), 999.0)
-            sig = binomial_test(cont, ref + cont)
-            b1, b2 = c1 // bin_size, c2 // bin_size
-            name = f"{f1[3] or 'none'};{f2[3] or 'none'}"
-            lines.append("\t".join(str(x) for x in (
-                f1[0], b1 * bin_size, (b1 + 1) * bin_size, f2[0], b2 * bin_size, (b2 + 1) * bin_size,
-                name, format(score, ".4G"), f1[4], f2[4], ref, cont, format(sig, ".4G"),
-                t["deletion"][0], t["deletion"][1], t["active_barriers"], len(t["barriers"]),
-                a0, a1, ws, we, t["cell_id"])))
+            pairs.append((f1, f2))
+    if not pairs:
+        return []
+    c1 = np.array([(f1[1] + f1[2] + 1) // 2 for f1, _ in pairs], dtype=np.int64)
+    c2 = np.array([(f2[1] + f2[2] + 1) // 2 for _, f2 in pairs], dtype=np.int64)
+    b1r, b2r = (c1 - ws) // bin_size, (c2 - ws) // bin_size
+    conts = band_blocks(result.band, nrows, ncols, b1r, b2r, block_size)
+    refs = band_blocks(ref_window_band, nrows, ncols, b1r, b2r, block_size)
+    lines = []
+    for k, (f1, f2) in enumerate(pairs):
+        cont, ref = int(conts[k]), int(refs[k])
+        if cont == 0 and ref == 0:
+            continue
+        if ref == 0:
+            score = 999.0
+        elif cont == 0:
+            score = -999.0
+        else:
+            score = min(max(float(np.log2(cont / ref)), -999.0), 999.0)
+        sig = binomial_test(cont, ref + cont)
+        b1, b2 = int(c1[k]) // bin_size, int(c2[k]) // bin_size
+        name = f"{f1[3] or 'none'};{f2[3] or 'none'}"
+        lines.append("\t".join(str(x) for x in (
+            f1[0], b1 * bin_size, (b1 + 1) * bin_size, f2[0], b2 * bin_size, (b2 + 1) * bin_size,
+            name, format(score, ".4G"), f1[4], f2[4], ref, cont, format(sig, ".4G"),
+            t["deletion"][0], t["deletion"][1], t["active_barriers"], len(t["barriers"]),
+            a0, a1, ws, we, t["cell_id"])))
     return lines

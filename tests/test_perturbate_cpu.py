@@ -2,6 +2,7 @@
 scheduler_common.cpp:51-127), restated in modlefork_gb300.perturbate."""
 
 import numpy as np
+import pytest
 
 from modlefork_gb300 import engine, genome, perturbate
 
@@ -120,3 +121,20 @@ def test_window_band_and_scores():
         assert r[13:] == ["30000", "31000", "2", "3", "20000", "40000", "20000", "60000", "7"]
     assert perturbate.binomial_test(5, 10) == 1.0
     assert abs(perturbate.binomial_test(0, 10) - 2 * 0.5 ** 10) < 1e-12
+
+
+@pytest.mark.parametrize("block_size", [1, 3, 4, 9])
+def test_vectorised_block_sums_equal_the_loop(block_size):
+    rng = np.random.default_rng(block_size)
+    nrows, ncols = 7, 40
+    band = rng.integers(0, 100, nrows * ncols).astype(np.uint32)
+    for j in range(ncols):
+        for r in range(nrows):
+            if r > j:
+                band[j * nrows + r] = 0
+    rows = rng.integers(0, ncols, 300)
+    cols = rng.integers(0, ncols, 300)
+    rows[:4], cols[:4] = [0, ncols - 1, 0, ncols - 1], [0, ncols - 1, ncols - 1, 0]
+    got = perturbate.band_blocks(band, nrows, ncols, rows, cols, block_size)
+    want = [perturbate.band_block(band, nrows, ncols, int(r), int(c), block_size) for r, c in zip(rows, cols)]
+    assert got.tolist() == want
