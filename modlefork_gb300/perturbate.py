@@ -55,8 +55,9 @@ def _features_in(features, lo, hi):
 
 def window_tasks(cfg, chrom, barriers, deletions, features=None):
     """Tasks of one chromosome in the reference's order: dicts with the window, the active
-    window, the deletion, the cell id, the LEF count, the contact and epoch targets and the
-    window's barriers with the deleted ones switched off."""
+    window, the deletion, the cell id (counted per chromosome, it seeds the cell), the task id
+    (counted over the whole run by simulate_windows; here equal to the cell id), the LEF count,
+    the contact and epoch targets and the window's barriers with the deleted ones switched off."""
     bars = sorted(barriers, key=lambda b: b["pos"])
     d = int(cfg.diagonal_width)
     bin_size = int(cfg.bin_size)
@@ -82,6 +83,7 @@ def window_tasks(cfg, chrom, barriers, deletions, features=None):
             nlefs = int(round((we - ws) / MBP * cfg.number_of_lefs_per_mbp))
             te = int(cfg.target_simulation_epochs) if target == 0 else (1 << 64) - 1
             tasks.append(dict(window=(ws, we), active=(a0, a1), deletion=(db, de), cell_id=cell_id,
+                              task_id=cell_id,
                               nlefs=nlefs, target_contacts=target, target_epochs=te, barriers=tb,
                               active_barriers=sum(1 for b in wbars if not (db <= b["pos"] < de))))
             cell_id += 1
@@ -114,6 +116,7 @@ def simulate_windows(cfg, genome, deletion_size=10_000, features=None, device=0,
             for t in window_tasks(cfg, chrom, bars, dels, feats):
                 if max_tasks is not None and len(batch) >= max_tasks:
                     break
+                t["task_id"] = len(meta)  # the run-wide task id (scheduler_perturbate.cpp:189, :298)
                 cid = eng.upload_window(chrom, t["window"][0], t["window"][1], t["barriers"])
                 nrows, ncols = engine.band_shape(cfg, t["window"][1] - t["window"][0])
                 bands[cid] = np.zeros(nrows * ncols, dtype=np.uint32)
@@ -205,8 +208,9 @@ def score_window(cfg, result, ref_window_band, feats1, feats2, block_size=9, las
     """bedpe records of one (window, deletion) task: for feature i of kind 1 and j >= i of kind
     2 (each (chrom, start, end, name, strand)), the block sums of the window's and the
     reference's contacts around their bins, their log2 ratio and binomial p-value, and the task's
-    window, deletion and barrier counts.  Pairs with both features past the partition point are
-    left to the next window (except in the last one), and pairs without contacts are skipped."""
+    window, deletion and barrier counts and its task id.  Pairs with both features past the
+    partition point are left to the next window (except in the last one), and pairs without
+    contacts are skipped."""
     t = result.task
     ws, we = t["window"]
     a0, a1 = t["active"]
@@ -245,5 +249,5 @@ def score_window(cfg, result, ref_window_band, feats1, feats2, block_size=9, las
             f1[0], b1 * bin_size, (b1 + 1) * bin_size, f2[0], b2 * bin_size, (b2 + 1) * bin_size,
             name, format(score, ".4G"), f1[4], f2[4], ref, cont, format(sig, ".4G"),
             t["deletion"][0], t["deletion"][1], t["active_barriers"], len(t["barriers"]),
-            a0, a1, ws, we, t["cell_id"])))
+            a0, a1, ws, we, t["task_id"])))
     return lines

@@ -103,7 +103,7 @@ def test_window_band_and_scores():
     for jr in range(wc):
         for r in range(min(wr, jr + 1)):
             assert win[jr * wr + r] == full[(4 + jr) * nrows + r]
-    task = dict(window=(20_000, 60_000), active=(20_000, 40_000), deletion=(30_000, 31_000), cell_id=7,
+    task = dict(window=(20_000, 60_000), active=(20_000, 40_000), deletion=(30_000, 31_000), cell_id=7, task_id=11,
                 active_barriers=2, barriers=[{}, {}, {}])
     sim = win.copy()
     sim[0] += 5
@@ -118,7 +118,7 @@ def test_window_band_and_scores():
         assert ref + cont > 0
         if ref and cont:
             assert abs(float(r[7]) - np.log2(cont / ref)) < 1e-3 * max(1.0, abs(np.log2(cont / ref)))
-        assert r[13:] == ["30000", "31000", "2", "3", "20000", "40000", "20000", "60000", "7"]
+        assert r[13:] == ["30000", "31000", "2", "3", "20000", "40000", "20000", "60000", "11"]
     assert perturbate.binomial_test(5, 10) == 1.0
     assert abs(perturbate.binomial_test(0, 10) - 2 * 0.5 ** 10) < 1e-12
 
