@@ -15,11 +15,22 @@ with a reference run's for every pair of features, as simulate_window's bedpe ou
 (block sums with edge extension, log2 ratio, two-sided binomial test).
 """
 
+import math
+
 import numpy as np
 
 from . import engine
 
 MBP = 1.0e6
+
+
+def cpp_round(x):
+    """std::round: halves go away from zero (Python's round sends them to the even neighbour)."""
+    x = float(x)
+    if x < 0:
+        return -cpp_round(-x)
+    f = math.floor(x)
+    return f + 1 if x - f >= 0.5 else f
 
 
 def generate_deletions(barriers, deletion_size):
@@ -79,8 +90,8 @@ def window_tasks(cfg, chrom, barriers, deletions, features=None):
             if cfg.target_contact_density != 0.0:
                 npix1 = (we - ws + bin_size - 1) // bin_size
                 npix2 = (d + bin_size - 1) // bin_size
-                target = int(max(1.0, round(cfg.target_contact_density * float(npix1 * npix2))))
-            nlefs = int(round((we - ws) / MBP * cfg.number_of_lefs_per_mbp))
+                target = int(max(1.0, cpp_round(cfg.target_contact_density * float(npix1 * npix2))))
+            nlefs = int(cpp_round((we - ws) / MBP * cfg.number_of_lefs_per_mbp))
             te = int(cfg.target_simulation_epochs) if target == 0 else (1 << 64) - 1
             tasks.append(dict(window=(ws, we), active=(a0, a1), deletion=(db, de), cell_id=cell_id,
                               task_id=cell_id,

@@ -138,3 +138,14 @@ def test_vectorised_block_sums_equal_the_loop(block_size):
     got = perturbate.band_blocks(band, nrows, ncols, rows, cols, block_size)
     want = [perturbate.band_block(band, nrows, ncols, int(r), int(c), block_size) for r, c in zip(rows, cols)]
     assert got.tolist() == want
+
+
+def test_task_sizes_round_halves_away_from_zero():
+    """The LEF count and contact target use std::round (scheduler_perturbate.cpp:306-320)."""
+    assert [perturbate.cpp_round(x) for x in (0.5, 1.5, 2.5, 2.4999999999999996, 60.5, -2.5, 0.0)] == \
+        [1, 2, 3, 2, 61, -3, 0]
+    cfg = genome.parity_config(diagonal_width=1_000_000, bin_size=5000, number_of_lefs_per_mbp=20.0)
+    chrom = engine.Chromosome("chrR", 3_025_000)  # the outer window is 3.025 Mbp: 60.5 LEFs
+    bars = [dict(pos=1_000_000, stp_active=0.9, stp_inactive=0.9, blocking_dir=1)]
+    tasks = perturbate.window_tasks(cfg, chrom, bars, perturbate.generate_deletions(bars, 10_000))
+    assert tasks[0]["window"] == (0, 3_025_000) and tasks[0]["nlefs"] == 61
