@@ -262,3 +262,112 @@ def score_window(cfg, result, ref_window_band, feats1, feats2, block_size=9, las
             t["deletion"][0], t["deletion"][1], t["active_barriers"], len(t["barriers"]),
             a0, a1, ws, we, t["task_id"])))
     return lines
+
+
+# ---------------------------------------------------------------------------------------------
+# the modle perturbate run: features, reference contacts, window tasks, bedpe records
+
+def read_bed_features(path):
+    """Features of a BED file as (chrom, start, end, name, strand) tuples grouped by chromosome
+    and sorted by (start, end): BED3-BED6 fields, name "" and strand "." when absent; track,
+    browser and comment lines are skipped (the --feature-beds inputs, cli.cpp:653-657)."""
+    import gzip
+
+    opener = gzip.open if str(path).endswith(".gz") else open
+    out = {}
+    with opener(path, "rt") as f:
+        for line in f:
+            if not line.strip() or line.startswith(("#", "track", "browser")):
+                continue
+            fs = line.rstrip("\n").split("\t")
+            if len(fs) < 3:
+                raise ValueError(f"{path}: a BED record needs at least 3 fields: {line!r}")
+            start, end = int(fs[1]), int(fs[2])
+            if end < start:
+                raise ValueError(f"{path}: end before start: {line!r}")
+            name = fs[3] if len(fs) > 3 else ""
+            strand = fs[5] if len(fs) > 5 else "."
+            out.setdefault(fs[0], []).append((fs[0], start, end, name, strand))
+    for v in out.values():
+        v.sort(key=lambda x: (x[1], x[2]))
+    return out
+
+
+def features_in(feats, lo, hi):
+    """The features overlapping [lo, hi) (map_features_to_window, scheduler_common.cpp:82-111)."""
+    return [f for f in feats if f[1] < hi and lo < f[2]]
+
+
+def perturbate_records(cfg, feats1, feats2, ref_bands, results, block_size=9):
+    """bedpe records of every window result, in task-id order: each window's features of both
+    kinds in its active window, scored against the reference run's band of its chromosome
+    restricted to the window.  ref_bands maps a chromosome name to its full band (chromosomes
+    simulated from position 0, as the generated workloads are)."""
+    lines = []
+    for r in results:
+        t = r.task
+        a0, a1 = t["active"]
+        ws, we = t["window"]
+        nrows_full, _ = engine.band_shape(cfg, r.chrom.simulated_size)
+        ref_win = window_band_of(cfg, ref_bands[r.chrom.name], nrows_full, ws, we)
+        f1 = features_in(feats1.get(r.chrom.name, []), a0, a1)
+        f2 = features_in(feats2.get(r.chrom.name, []), a0, a1)
+        lines += score_window(cfg, r, ref_win, f1, f2, block_size=block_size,
+                              last_window=a1 == r.chrom.end)
+    return lines
+
+
+def write_bedpe(path, lines):
+    import gzip
+
+    opener = gzip.open if str(path).endswith(".gz") else open
+    with opener(path, "wt") as f:
+        for ln in lines:
+            f.write(ln + "\n")
+
+
+def _main(argv=None):
+    """modle perturbate on a generated workload: a reference run of the whole genome, then one
+    cell per (window, deletion) in one batched launch, scored for every pair of features of the
+    two BED files.  Example:
+
+    python -m modlefork_gb300.perturbate --workload parity --features a.bed b.bed --out x.bedpe.gz
+    """
+    import argparse
+    import json
+    import time
+
+    from . import genome as gen
+    from .simulate import simulate_genome_batched
+
+    ap = argparse.ArgumentParser(description=_main.__doc__)
+    ap.add_argument("--workload", choices=["parity", "genome"], default="parity")
+    ap.add_argument("--chroms", type=int, default=24, help="chromosomes of the generated genome workload")
+    ap.add_argument("--features", nargs=2, required=True, metavar=("BED1", "BED2"))
+    ap.add_argument("--deletion-size", type=int, default=10_000)
+    ap.add_argument("--block-size", type=int, default=9)
+    ap.add_argument("--max-tasks", type=int, default=None)
+    ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--out", required=True, help="bedpe output (gzip when it ends in .gz)")
+    args = ap.parse_args(argv)
+    if args.block_size < 1 or args.block_size % 2 == 0:
+        ap.error("--block-size must be a positive odd number")
+    cfg, g = gen.parity_10mbp() if args.workload == "parity" else gen.genome_24chr(nchroms=args.chroms)
+    feats1, feats2 = read_bed_features(args.features[0]), read_bed_features(args.features[1])
+    names = {c.name for c, _ in g}
+    features = {n: ([(f[1], f[2]) for f in feats1[n]], [(f[1], f[2]) for f in feats2[n]])
+                for n in names if n in feats1 and n in feats2}
+    t0 = time.perf_counter()
+    ref = {r.chrom.name: r.band for r in simulate_genome_batched(cfg, g, device=args.device)}
+    t1 = time.perf_counter()
+    results = simulate_windows(cfg, g, args.deletion_size, features, device=args.device,
+                               max_tasks=args.max_tasks)
+    t2 = time.perf_counter()
+    lines = perturbate_records(cfg, feats1, feats2, ref, results, args.block_size)
+    write_bedpe(args.out, lines)
+    print(json.dumps({"workload": args.workload, "tasks": len(results), "records": len(lines),
+                      "reference_s": t1 - t0, "windows_s": t2 - t1, "scoring_s": time.perf_counter() - t2}))
+
+
+if __name__ == "__main__":
+    _main()

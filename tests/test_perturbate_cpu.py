@@ -149,3 +149,62 @@ def test_task_sizes_round_halves_away_from_zero():
     bars = [dict(pos=1_000_000, stp_active=0.9, stp_inactive=0.9, blocking_dir=1)]
     tasks = perturbate.window_tasks(cfg, chrom, bars, perturbate.generate_deletions(bars, 10_000))
     assert tasks[0]["window"] == (0, 3_025_000) and tasks[0]["nlefs"] == 61
+
+
+def test_read_bed_features(tmp_path):
+    import gzip
+
+    text = "track name=x\n#c\nchr2\t50\t60\tb\t0\t-\nchr1\t10\t20\nchr1\t5\t8\ta\t1\t+\n"
+    p = tmp_path / "f.bed"
+    p.write_text(text)
+    pz = tmp_path / "f.bed.gz"
+    with gzip.open(pz, "wt") as f:
+        f.write(text)
+    for path in (p, pz):
+        got = perturbate.read_bed_features(str(path))
+        assert got == {"chr1": [("chr1", 5, 8, "a", "+"), ("chr1", 10, 20, "", ".")],
+                       "chr2": [("chr2", 50, 60, "b", "-")]}
+    bad = tmp_path / "bad.bed"
+    bad.write_text("chr1\t10\n")
+    with pytest.raises(ValueError):
+        perturbate.read_bed_features(str(bad))
+
+
+def test_records_take_the_active_window_features(tmp_path):
+    """perturbate_records scores each window with the features of its active window, against
+    the reference band restricted to the window, and writes (gzipped) bedpe."""
+    cfg = genome.parity_config(diagonal_width=20_000, bin_size=5000)
+    chrom = engine.Chromosome("chrW", 100_000)
+    nrows, ncols = engine.band_shape(cfg, chrom.size)
+    rng = np.random.default_rng(5)
+    ref = rng.integers(0, 9, nrows * ncols).astype(np.uint32)
+    feats1 = {"chrW": [("chrW", 15_000, 15_001, "a", "+"), ("chrW", 75_000, 75_001, "c", "+")]}
+    feats2 = {"chrW": [("chrW", 24_000, 24_001, "", "-"), ("chrW", 35_000, 35_001, "b", "+"),
+                       ("chrW", 78_000, 78_001, "d", "-")]}
+    results = []
+    for tid, (ws, we, a0, a1) in enumerate([(0, 80_000, 0, 60_000), (20_000, 100_000, 40_000, 100_000)]):
+        wr, wc = engine.band_shape(cfg, we - ws)
+        task = dict(window=(ws, we), active=(a0, a1), deletion=(30_000, 31_000), cell_id=tid, task_id=tid,
+                    active_barriers=1, barriers=[{}, {}])
+        results.append(perturbate.WindowResult(chrom, task, rng.integers(0, 9, wr * wc).astype(np.uint32), None))
+    lines = perturbate.perturbate_records(cfg, feats1, feats2, {"chrW": ref}, results, block_size=3)
+    want = []
+    for r in results:
+        a0, a1 = r.task["active"]
+        ws, we = r.task["window"]
+        win = perturbate.window_band_of(cfg, ref, nrows, ws, we)
+        f1 = [f for f in feats1["chrW"] if a0 <= f[1] < a1]
+        f2 = [f for f in feats2["chrW"] if a0 <= f[1] < a1]
+        want += perturbate.score_window(cfg, r, win, f1, f2, block_size=3, last_window=a1 == chrom.end)
+    assert lines == want and lines
+    assert {ln.split("\t")[-1] for ln in lines} <= {"0", "1"}
+    # the first window pairs feature a with the kind-2 features of its active window; the
+    # second (the last window of the chromosome) pairs c with d
+    names = [(ln.split("\t")[6], ln.split("\t")[-1]) for ln in lines]
+    assert {n for n, t in names if t == "0"} <= {"a;none", "a;b"} and {n for n, t in names if t == "1"} <= {"c;d"}
+    out = tmp_path / "x.bedpe.gz"
+    perturbate.write_bedpe(str(out), lines)
+    import gzip
+
+    with gzip.open(out, "rt") as f:
+        assert f.read().splitlines() == lines
