@@ -317,11 +317,21 @@ def perturbate_records(cfg, feats1, feats2, ref_bands, results, block_size=9):
     return lines
 
 
-def write_bedpe(path, lines):
+# bedpe columns, the header line the reference writes when asked to (scheduler_perturbate.cpp:120-152)
+BEDPE_COLUMNS = ("chrom1", "start1", "end1", "chrom2", "start2", "end2", "name", "score", "strand1",
+                 "strand2", "reference_contacts", "contacts", "significance", "deletion_begin",
+                 "deletion_end", "num_active_barriers", "total_num_barriers", "active_window_start",
+                 "active_window_end", "window_start", "window_end", "task_id")
+
+
+def write_bedpe(path, lines, header=True):
+    """bedpe records (gzip when the path ends in .gz), after a '#'-prefixed column header."""
     import gzip
 
     opener = gzip.open if str(path).endswith(".gz") else open
     with opener(path, "wt") as f:
+        if header:
+            f.write("#" + "\t".join(BEDPE_COLUMNS) + "\n")
         for ln in lines:
             f.write(ln + "\n")
 
@@ -349,6 +359,7 @@ def _main(argv=None):
     ap.add_argument("--max-tasks", type=int, default=None)
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--out", required=True, help="bedpe output (gzip when it ends in .gz)")
+    ap.add_argument("--no-header", action="store_true", help="omit the bedpe column header")
     args = ap.parse_args(argv)
     if args.block_size < 1 or args.block_size % 2 == 0:
         ap.error("--block-size must be a positive odd number")
@@ -364,7 +375,7 @@ def _main(argv=None):
                                max_tasks=args.max_tasks)
     t2 = time.perf_counter()
     lines = perturbate_records(cfg, feats1, feats2, ref, results, args.block_size)
-    write_bedpe(args.out, lines)
+    write_bedpe(args.out, lines, header=not args.no_header)
     print(json.dumps({"workload": args.workload, "tasks": len(results), "records": len(lines),
                       "reference_s": t1 - t0, "windows_s": t2 - t1, "scoring_s": time.perf_counter() - t2}))
 

@@ -8,9 +8,16 @@ without barriers are skipped unless ``simulate_chromosomes_wo_barriers`` is set
 (scheduler_simulate.cpp:114-121).
 """
 
+import gzip
+
 import numpy as np
 
 from . import engine
+
+
+def _open_text(path):
+    """A text file for writing, gzip-compressed when the path ends in .gz."""
+    return gzip.open(path, "wt") if str(path).endswith(".gz") else open(path, "w")
 
 
 class ChromResult:
@@ -136,7 +143,7 @@ def write_lef_occupancy(path, cfg, results):
     simulation.cpp:214-262): each chromosome's counters divided by its maximum, as float32, one
     interval per bin from the chromosome's start."""
     bin_size = int(cfg.bin_size)
-    with open(path, "w") as f:
+    with _open_text(path) as f:
         for r in results:
             if r.occupancy is None:
                 continue
@@ -176,7 +183,7 @@ def write_model_state(path, results):
     task, epoch, cell, chrom, burn-in, effective barrier occupancy, LEFs, stalled rev / fwd /
     both, LEF-BAR, primary and secondary LEF-LEF collisions, mean loop size.  The task id is the
     chromosome's index in the run times the cell count plus the cell."""
-    with open(path, "w") as f:
+    with _open_text(path) as f:
         for ci, r in enumerate(results):
             if r.records is None:
                 continue
@@ -259,7 +266,7 @@ def _main(argv=None):
     dt = time.perf_counter() - t0
     if args.pixels:
         b1, b2, cnt = genome_pixels(cfg, res, [c for c, _ in g])
-        with open(args.pixels, "w") as f:
+        with _open_text(args.pixels) as f:
             f.write("bin1_id\tbin2_id\tcount\n")
             for a, b, c in zip(b1.tolist(), b2.tolist(), cnt.tolist()):
                 f.write(f"{a}\t{b}\t{c}\n")

@@ -207,4 +207,6 @@ def test_records_take_the_active_window_features(tmp_path):
     import gzip
 
     with gzip.open(out, "rt") as f:
-        assert f.read().splitlines() == lines
+        got = f.read().splitlines()
+    assert got[0] == "#" + "\t".join(perturbate.BEDPE_COLUMNS) and got[1:] == lines
+    assert all(len(ln.split("\t")) == len(perturbate.BEDPE_COLUMNS) for ln in lines)
