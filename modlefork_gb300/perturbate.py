@@ -109,37 +109,49 @@ class WindowResult:
         self.stats = stats
 
 
+def plan_windows(cfg, genome, deletion_size=10_000, features=None, max_tasks=None):
+    """Every (window, deletion) task of the genome in the reference's order, as (chrom, task)
+    pairs with run-wide task ids (scheduler_perturbate.cpp:189, :298).  ``features`` maps a
+    chromosome name to two lists of (start, end) intervals (the two feature kinds); chromosomes
+    without barriers, or without features when ``features`` is given, are skipped, and without
+    it no window is skipped for lack of features."""
+    planned = []
+    for chrom, bars in genome:
+        if not bars:
+            continue
+        feats = features.get(chrom.name) if features is not None else None
+        if features is not None and feats is None:
+            continue
+        for t in window_tasks(cfg, chrom, bars, generate_deletions(bars, deletion_size), feats):
+            if max_tasks is not None and len(planned) >= max_tasks:
+                return planned
+            t["task_id"] = len(planned)
+            planned.append((chrom, t))
+    return planned
+
+
+def run_windows(cfg, planned, device=0):
+    """Simulate the planned (chrom, task) pairs in one batched launch (mgpu_upload_window per
+    task, mgpu_simulate_batch); returns one WindowResult per task, in the given order."""
+    if not planned:
+        return []
+    with engine.Engine(cfg, device) as eng:
+        batch, bands, cids = [], {}, []
+        for chrom, t in planned:
+            cid = eng.upload_window(chrom, t["window"][0], t["window"][1], t["barriers"])
+            nrows, ncols = engine.band_shape(cfg, t["window"][1] - t["window"][0])
+            bands[cid] = np.zeros(nrows * ncols, dtype=np.uint32)
+            seed = engine.cell_seed(chrom.name, chrom.size, cfg.seed, t["cell_id"])
+            batch.append((cid, seed, t["target_contacts"], t["target_epochs"], t["nlefs"]))
+            cids.append(cid)
+        _, stats = eng.simulate_batch(batch, bands)
+    return [WindowResult(chrom, t, bands[cid], stats[k]) for k, ((chrom, t), cid) in enumerate(zip(planned, cids))]
+
+
 def simulate_windows(cfg, genome, deletion_size=10_000, features=None, device=0, max_tasks=None):
     """Simulate every (window, deletion) task of the genome in one batched launch; returns one
-    WindowResult per task, in task-id order.  ``features`` maps a chromosome name to two lists
-    of (start, end) intervals (the two feature kinds); without it no window is skipped for
-    lack of features."""
-    results = []
-    with engine.Engine(cfg, device) as eng:
-        batch, bands, meta = [], {}, []
-        for chrom, bars in genome:
-            if not bars:
-                continue
-            dels = generate_deletions(bars, deletion_size)
-            feats = features.get(chrom.name) if features is not None else None
-            if features is not None and feats is None:
-                continue
-            for t in window_tasks(cfg, chrom, bars, dels, feats):
-                if max_tasks is not None and len(batch) >= max_tasks:
-                    break
-                t["task_id"] = len(meta)  # the run-wide task id (scheduler_perturbate.cpp:189, :298)
-                cid = eng.upload_window(chrom, t["window"][0], t["window"][1], t["barriers"])
-                nrows, ncols = engine.band_shape(cfg, t["window"][1] - t["window"][0])
-                bands[cid] = np.zeros(nrows * ncols, dtype=np.uint32)
-                seed = engine.cell_seed(chrom.name, chrom.size, cfg.seed, t["cell_id"])
-                batch.append((cid, seed, t["target_contacts"], t["target_epochs"], t["nlefs"]))
-                meta.append((chrom, t, cid))
-        if not batch:
-            return results
-        _, stats = eng.simulate_batch(batch, bands)
-    for k, (chrom, t, cid) in enumerate(meta):
-        results.append(WindowResult(chrom, t, bands[cid], stats[k]))
-    return results
+    WindowResult per task, in task-id order (plan_windows, then run_windows)."""
+    return run_windows(cfg, plan_windows(cfg, genome, deletion_size, features, max_tasks), device)
 
 
 # ---------------------------------------------------------------------------------------------

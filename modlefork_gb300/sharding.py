@@ -1,4 +1,4 @@
-"""Multi-GPU runs: one process per GPU, cells sharded across ranks.
+"""Multi-GPU runs: one process per GPU, cells (or perturbate windows) sharded across ranks.
 
 A cell is a pure function of the configuration, the chromosome and its cell id (its seed is
 Chromosome::hash of (seed, cell id), genome.cpp:317-335), so ranks share nothing while they
@@ -66,3 +66,37 @@ def simulate_chromosome_sharded(run_cells, chrom_task, world, rank, device=None,
     band = allreduce_counts(band, device, group)
     missed = int(allreduce_counts(np.array([missed], dtype=np.uint64), device, group)[0])
     return band, missed
+
+
+def shard_windows(planned, world, rank):
+    """The contiguous block of the window queue (perturbate.plan_windows' (chrom, task) pairs,
+    in task-id order) that ``rank`` simulates."""
+    lo, hi = cell_range(len(planned), world, rank)
+    return planned[lo:hi]
+
+
+def gather_records(records, group=None):
+    """Every rank's (task_id, bedpe line) records, merged in task-id order (records of one task
+    keep their order); every rank returns the merged lines."""
+    import torch.distributed as dist
+
+    parts = [None] * dist.get_world_size(group)
+    dist.all_gather_object(parts, list(records), group=group)
+    merged = sorted((r for part in parts for r in part), key=lambda r: r[0])
+    return [line for _, line in merged]
+
+
+def perturbate_sharded(cfg, planned, feats1, feats2, ref_bands, world, rank, run_windows, block_size=9,
+                       group=None):
+    """modle perturbate over ranks: this rank simulates its block of the window queue with
+    ``run_windows(cfg, planned_block)`` (perturbate.run_windows on a GPU), scores its windows,
+    and the ranks exchange their records; each rank returns all records in task-id order.
+    Window cells are independent, so only the records cross ranks."""
+    from . import perturbate
+
+    mine = shard_windows(planned, world, rank)
+    recs = []
+    for r in run_windows(cfg, mine):
+        for line in perturbate.perturbate_records(cfg, feats1, feats2, ref_bands, [r], block_size):
+            recs.append((r.task["task_id"], line))
+    return gather_records(recs, group)

@@ -102,3 +102,86 @@ def test_two_gloo_ranks_equal_one_process():
         assert np.array_equal(b, want)
         assert m[0] == missed
         assert m[1] == 11.0 and m[2] == 6 and m[3] == 300
+
+
+# ---------------------------------------------------------------------------------------------
+# perturbate: the window queue sharded over ranks, records gathered in task-id order
+
+def _window_case():
+    from modlefork_gb300 import engine, genome, perturbate
+
+    cfg = genome.parity_config(diagonal_width=500_000)
+    rng = np.random.default_rng(12)
+    gen, feats1, feats2 = [], {}, {}
+    for k, L in enumerate((2_400_000, 1_800_000)):
+        ch = engine.Chromosome(f"chrQ{k}", L)
+        gen.append((ch, engine.barriers_from_bed(ch, genome.bed_records(rng, L, 30), 0.7, 0.7)))
+        for feats, tag in ((feats1, "a"), (feats2, "b")):
+            pos = np.sort(rng.integers(0, L - 1000, 25))
+            feats[ch.name] = [(ch.name, int(p), int(p) + 500, f"{tag}{i}", "+") for i, p in enumerate(pos)]
+    features = {n: ([(f[1], f[2]) for f in feats1[n]], [(f[1], f[2]) for f in feats2[n]]) for n in feats1}
+    planned = perturbate.plan_windows(cfg, gen, deletion_size=60_000, features=features, max_tasks=10)
+    ref = {}
+    for ch, _ in gen:
+        nrows, ncols = engine.band_shape(cfg, ch.simulated_size)
+        ref[ch.name] = rng.integers(0, 5, nrows * ncols).astype(np.uint32)
+    return cfg, planned, feats1, feats2, ref
+
+
+def _oracle_windows(cfg, planned):
+    """perturbate.run_windows with the oracle's window cell as the engine."""
+    from _harness import load_oracle, make_chrom
+    from modlefork_gb300 import _abi as abi
+    from modlefork_gb300 import engine, perturbate
+
+    lib = load_oracle()
+    out = []
+    for chrom, t in planned:
+        ws, we = t["window"]
+        nrows, ncols = engine.band_shape(cfg, we - ws)
+        band = np.zeros(nrows * ncols, dtype=np.uint32)
+        st = abi.CellStats()
+        ch = make_chrom(chrom.start, chrom.end, chrom.size, chrom.name.encode())
+        seed = engine.cell_seed(chrom.name, chrom.size, cfg.seed, t["cell_id"])
+        rc = lib.orc_simulate_window_cell(C.byref(cfg), C.byref(ch), ws, we, abi.make_barriers(t["barriers"]),
+                                          len(t["barriers"]), seed, t["target_contacts"], t["target_epochs"],
+                                          t["nlefs"], band.ctypes.data_as(C.POINTER(C.c_uint32)), C.byref(st))
+        assert rc == 0
+        out.append(perturbate.WindowResult(chrom, t, band, st))
+    return out
+
+
+def _window_rank_main(rank, world, port, outdir):
+    import sys
+
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    import torch.distributed as dist
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        cfg, planned, feats1, feats2, ref = _window_case()
+        lines = sharding.perturbate_sharded(cfg, planned, feats1, feats2, ref, world, rank, _oracle_windows,
+                                            block_size=3)
+        with open(os.path.join(outdir, f"rec{rank}.txt"), "w") as f:
+            f.write("\n".join(lines))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_window_queue_over_two_gloo_ranks_equals_one_process():
+    import torch.multiprocessing as mp
+
+    from modlefork_gb300 import perturbate
+
+    world = 2
+    with tempfile.TemporaryDirectory() as d:
+        mp.start_processes(_window_rank_main, args=(world, _free_port(), d), nprocs=world, start_method="spawn",
+                           join=True)
+        got = [open(os.path.join(d, f"rec{r}.txt")).read().split("\n") for r in range(world)]
+    cfg, planned, feats1, feats2, ref = _window_case()
+    assert len(planned) == 10 and len({t["task_id"] for _, t in planned}) == 10
+    assert [t["task_id"] for _, t in sharding.shard_windows(planned, 2, 1)] == list(range(5, 10))
+    want = perturbate.perturbate_records(cfg, feats1, feats2, ref, _oracle_windows(cfg, planned), block_size=3)
+    assert want and got[0] == want and got[1] == want
