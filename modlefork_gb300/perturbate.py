@@ -109,12 +109,15 @@ class WindowResult:
         self.stats = stats
 
 
-def plan_windows(cfg, genome, deletion_size=10_000, features=None, max_tasks=None):
+def plan_windows(cfg, genome, deletion_size=10_000, features=None, max_tasks=None, deletions=None):
     """Every (window, deletion) task of the genome in the reference's order, as (chrom, task)
     pairs with run-wide task ids (scheduler_perturbate.cpp:189, :298).  ``features`` maps a
     chromosome name to two lists of (start, end) intervals (the two feature kinds); chromosomes
     without barriers, or without features when ``features`` is given, are skipped, and without
-    it no window is skipped for lack of features."""
+    it no window is skipped for lack of features.  ``deletions`` maps a chromosome name to its
+    (start, end) deletions (an imported --deletion-list, Simulation::import_deletions,
+    scheduler_common.cpp:42-49); chromosomes it lacks are skipped.  Without it the deletions are
+    generated from the barriers (generate_deletions)."""
     planned = []
     for chrom, bars in genome:
         if not bars:
@@ -122,7 +125,13 @@ def plan_windows(cfg, genome, deletion_size=10_000, features=None, max_tasks=Non
         feats = features.get(chrom.name) if features is not None else None
         if features is not None and feats is None:
             continue
-        for t in window_tasks(cfg, chrom, bars, generate_deletions(bars, deletion_size), feats):
+        if deletions is not None:
+            if chrom.name not in deletions:
+                continue
+            dels = sorted((int(a), int(b)) for a, b in deletions[chrom.name])
+        else:
+            dels = generate_deletions(bars, deletion_size)
+        for t in window_tasks(cfg, chrom, bars, dels, feats):
             if max_tasks is not None and len(planned) >= max_tasks:
                 return planned
             t["task_id"] = len(planned)
@@ -279,6 +288,12 @@ def score_window(cfg, result, ref_window_band, feats1, feats2, block_size=9, las
 # ---------------------------------------------------------------------------------------------
 # the modle perturbate run: features, reference contacts, window tasks, bedpe records
 
+def read_bed_intervals(path):
+    """BED3 intervals grouped by chromosome: {chrom: [(start, end)]} sorted, e.g. a deletion
+    list (bed::BED_tree of BED3 records)."""
+    return {c: [(f[1], f[2]) for f in fs] for c, fs in read_bed_features(path).items()}
+
+
 def read_bed_features(path):
     """Features of a BED file as (chrom, start, end, name, strand) tuples grouped by chromosome
     and sorted by (start, end): BED3-BED6 fields, name "" and strand "." when absent; track,
@@ -366,7 +381,9 @@ def _main(argv=None):
     ap.add_argument("--workload", choices=["parity", "genome"], default="parity")
     ap.add_argument("--chroms", type=int, default=24, help="chromosomes of the generated genome workload")
     ap.add_argument("--features", nargs=2, required=True, metavar=("BED1", "BED2"))
-    ap.add_argument("--deletion-size", type=int, default=10_000)
+    dg = ap.add_mutually_exclusive_group()
+    dg.add_argument("--deletion-size", type=int, default=10_000)
+    dg.add_argument("--deletion-list", default=None, help="BED file of the deletions to perform")
     ap.add_argument("--block-size", type=int, default=9)
     ap.add_argument("--max-tasks", type=int, default=None)
     ap.add_argument("--device", type=int, default=0)
@@ -383,8 +400,9 @@ def _main(argv=None):
     t0 = time.perf_counter()
     ref = {r.chrom.name: r.band for r in simulate_genome_batched(cfg, g, device=args.device)}
     t1 = time.perf_counter()
-    results = simulate_windows(cfg, g, args.deletion_size, features, device=args.device,
-                               max_tasks=args.max_tasks)
+    dels = read_bed_intervals(args.deletion_list) if args.deletion_list else None
+    results = run_windows(cfg, plan_windows(cfg, g, args.deletion_size, features, args.max_tasks, dels),
+                          device=args.device)
     t2 = time.perf_counter()
     lines = perturbate_records(cfg, feats1, feats2, ref, results, args.block_size)
     write_bedpe(args.out, lines, header=not args.no_header)

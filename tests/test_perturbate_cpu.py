@@ -210,3 +210,28 @@ def test_records_take_the_active_window_features(tmp_path):
         got = f.read().splitlines()
     assert got[0] == "#" + "\t".join(perturbate.BEDPE_COLUMNS) and got[1:] == lines
     assert all(len(ln.split("\t")) == len(perturbate.BEDPE_COLUMNS) for ln in lines)
+
+
+def test_plan_windows_with_a_deletion_list(tmp_path):
+    cfg = genome.parity_config(diagonal_width=500_000)
+    chroms = [engine.Chromosome("chrD0", 2_000_000), engine.Chromosome("chrD1", 1_500_000)]
+    rng = np.random.default_rng(6)
+    gen = [(ch, engine.barriers_from_bed(ch, genome.bed_records(rng, ch.size, 12), 0.7, 0.7)) for ch in chroms]
+    bed = tmp_path / "del.bed"
+    bed.write_text("chrD0\t900000\t950000\nchrD0\t100000\t120000\nchrX\t1\t5\n")
+    dels = perturbate.read_bed_intervals(str(bed))
+    assert dels == {"chrD0": [(100_000, 120_000), (900_000, 950_000)], "chrX": [(1, 5)]}
+    planned = perturbate.plan_windows(cfg, gen, deletions=dels)
+    # chrD1 has no deletions and is skipped; every task carries one of the listed deletions
+    assert {c.name for c, _ in planned} == {"chrD0"}
+    assert {t["deletion"] for _, t in planned} <= set(dels["chrD0"])
+    assert [t["task_id"] for _, t in planned] == list(range(len(planned)))
+    for _, t in planned:
+        ws, we = t["window"]
+        db, de = t["deletion"]
+        assert db < we and ws < de  # the deletion overlaps the window
+        off = [b for b in t["barriers"] if b["stp_active"] == 0.0 and b["stp_inactive"] == 1.0]
+        assert len(t["barriers"]) - len(off) == t["active_barriers"]
+    # generated deletions: one per barrier, ending one bp after it
+    gen_plan = perturbate.plan_windows(cfg, gen, deletion_size=30_000)
+    assert {c.name for c, _ in gen_plan} == {"chrD0", "chrD1"}
