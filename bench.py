@@ -47,7 +47,9 @@ def parse_args():
     ap.add_argument("--cells", type=int, default=512, help="cells per chromosome")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline time budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--serial-every", type=int, default=3,
+                    help="plain path one launch at a time over every n-th chromosome (0 = skip)")
     ap.add_argument("--workers", type=int, default=24, help="concurrent engine contexts")
     ap.add_argument("--wave", type=int, default=24, help="chromosome launches per step")
     ap.add_argument("--smem-budget", type=int, default=None, help="shared memory per cell (bytes)")
@@ -139,19 +141,24 @@ def dram_traffic_per_launch(lef_epochs_per_launch, kernel="simulate_kernel"):
 
 
 # ---------------------------------------------------------------------------------------------
-def build_workload(cells, rank):
-    from modlefork_gb300 import engine, genome
+def build_workload(cells, rank, api=None):
+    """The genome workload's tasks.  ``api`` answers the host helpers (seeds, LEF counts, task
+    targets, band shapes): the engine for our arm, the oracle's helpers for the CPU arm, which
+    must not load the product library."""
+    from modlefork_gb300 import genome
 
-    cfg, gen = genome.genome_24chr(seed=11)
+    if api is None:
+        from modlefork_gb300 import engine as api
+    cfg, gen = genome.genome_24chr(seed=11, api=api)
     tasks = []
     for chrom, bars in gen:
         size = chrom.simulated_size
-        nl = engine.num_lefs(cfg, size)
-        targets, te = engine.task_targets(cfg, size, nl, cells)
+        nl = api.num_lefs(cfg, size)
+        targets, te = api.task_targets(cfg, size, nl, cells)
         base = rank * cells  # weak scaling: each rank simulates its own cell ids
-        seeds = np.array([engine.cell_seed(chrom.name, chrom.size, cfg.seed, base + i) for i in range(cells)],
+        seeds = np.array([api.cell_seed(chrom.name, chrom.size, cfg.seed, base + i) for i in range(cells)],
                          dtype=np.uint64)
-        nrows, ncols = engine.band_shape(cfg, size)
+        nrows, ncols = api.band_shape(cfg, size)
         tasks.append(dict(chrom=chrom, bars=bars, nlefs=nl, targets=targets, te=te, seeds=seeds,
                           nrows=nrows, ncols=ncols))
     return cfg, tasks
@@ -177,6 +184,7 @@ def cpu_sample(cfg, task, budget_s, threads):
     ch = make_chrom(chrom.start, chrom.end, chrom.size, chrom.name.encode())
     band = np.zeros(task["nrows"] * task["ncols"], dtype=np.uint32)
     done_cells = lef_epochs = contacts = 0
+    per_cell = []
     t0 = time.perf_counter()
     i0 = 0
     while i0 < len(task["seeds"]) and (done_cells == 0 or time.perf_counter() - t0 < budget_s):
@@ -195,9 +203,10 @@ def cpu_sample(cfg, task, budget_s, threads):
         done_cells += n
         lef_epochs += sum(s.lef_epochs for s in st)
         contacts += sum(s.contacts for s in st)
+        per_cell += [(i0 + j, st[j].epochs, st[j].contacts, st[j].rng_draws, st[j].lef_epochs) for j in range(n)]
         i0 += n
     dt = time.perf_counter() - t0
-    return dict(seconds=dt, cells=done_cells, lef_epochs=lef_epochs, contacts=contacts,
+    return dict(seconds=dt, cells=done_cells, lef_epochs=lef_epochs, contacts=contacts, per_cell=per_cell,
                 sample=f"{chrom.name} ({chrom.size / 1e6:.1f} Mbp, {task['nlefs']} LEFs, "
                        f"{len(task['bars'])} barriers): cells 0..{done_cells - 1} of {len(task['seeds'])}, "
                        f"{threads} threads")
@@ -207,13 +216,14 @@ def cpu_sample_genome(cfg, tasks, budget_s, threads, first=0):
     """Time the oracle on the genome's mix: one batch of ``threads`` whole cells from each
     chromosome in turn (chromosome ``first`` onwards, largest and smallest alike) until the
     budget is spent."""
-    total = dict(seconds=0.0, cells=0, lef_epochs=0, contacts=0)
+    total = dict(seconds=0.0, cells=0, lef_epochs=0, contacts=0, per_cell={})
     names, k = [], first
     while total["seconds"] < budget_s and len(names) < len(tasks):
         t = tasks[k % len(tasks)]
         s = cpu_sample(cfg, t, 0.0, threads)  # one batch
         for key in ("seconds", "cells", "lef_epochs", "contacts"):
             total[key] += s[key]
+        total["per_cell"][k % len(tasks)] = s["per_cell"]
         names.append(t["chrom"].name)
         k += 1
     total["sample"] = (f"{threads} whole cells (ids 0..{threads - 1}) of each of {len(names)} chromosomes "
@@ -227,10 +237,12 @@ def run_reference(args):
     world, rank, _ = dist_env()
     if world > 1 and rank != 0:
         return
-    from modlefork_gb300 import build as mbuild
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _harness import OracleHelpers
 
-    mbuild.build()
-    cfg, tasks = build_workload(args.cells, 0)
+    # the workload's seeds, targets and barriers come from the oracle's own helpers: this arm
+    # loads liboracle.so and nothing of the product
+    cfg, tasks = build_workload(args.cells, 0, api=OracleHelpers())
     threads = os.cpu_count() or 1
     per_step = max(1.0, args.cpu_seconds / 2)
     for _ in range(args.warmup):
@@ -247,7 +259,10 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64+f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_per_step": samples[0]["sample"]},
+        "config": {"workload": WORKLOAD, "sample_per_step": samples[0]["sample"],
+                   "same_config_note": "the same genome workload as our arm; each step times a bounded "
+                                       "sample of it (whole cells of every chromosome in turn), so the "
+                                       "rate is comparable while the cells timed are a subset"},
         "cpu_baseline": {"value": value, "unit": "LEF-epochs/s", "cores": threads, "kind": "port",
                          "sample": samples[0]["sample"]},
         "e2e": {"value": value, "unit": "LEF-epochs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -385,19 +400,26 @@ def run_ours(args):
         for t in tasks:
             t["h_band"] = np.zeros(t["nrows"] * t["ncols"], dtype=np.uint32)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        edone = []
+        edone, step_rates, dt = [], [], 0.0
         for i in range(args.e2e_steps):
-            edone += run_wave(i, False)
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
+            log(f"e2e step {i}")
+            t0 = time.perf_counter()
+            sdone = run_wave(i, False)
+            torch.cuda.synchronize()
+            sdt = time.perf_counter() - t0
+            dt += sdt
+            step_rates.append(tally(sdone)["lef_epochs"] / sdt)
+            edone += sdone
         eagg = tally(edone)
         h2d = sum(tasks[k]["seeds"].nbytes + tasks[k]["targets"].nbytes + tasks[k]["h_band"].nbytes
                   for k, _, _ in edone)
         d2h = sum(tasks[k]["h_band"].nbytes + len(st) * C.sizeof(st[0]) for k, st, _ in edone)
         e2e = {"value": eagg["lef_epochs"] / dt, "unit": "LEF-epochs/s",
                "h2d_bytes_per_step": h2d // args.e2e_steps, "d2h_bytes_per_step": d2h // args.e2e_steps,
-               "steps": args.e2e_steps, "cells_per_s": eagg["cells"] / dt}
+               "steps": args.e2e_steps, "cells_per_s": eagg["cells"] / dt,
+               "step_rates": {"min": min(step_rates), "median": statistics.median(step_rates),
+                              "max": max(step_rates)},
+               "timing": "host clock around each step's C-ABI calls and a device synchronisation"}
 
     # batched: the whole genome in one launch and work queue (mgpu_simulate_batch)
     batched = None
@@ -434,6 +456,46 @@ def run_ours(args):
                    "e2e": {"value": sum(x.lef_epochs for x in bst2) / bdt, "unit": "LEF-epochs/s",
                            "h2d_bytes_per_step": int(sum(b.nbytes for b in hb.values()) + len(btasks) * 40),
                            "d2h_bytes_per_step": int(sum(b.nbytes for b in hb.values()) + len(btasks) * 64)}}
+
+    # the plain path one launch at a time: one context, every n-th chromosome's 512 cells in
+    # one blocking call after another (the reference's drop-in used from a single worker), and
+    # the batched engine on exactly the same cells
+    serial = None
+    if args.serial_every > 0:
+        w0 = workers[0]
+        w0["eng"].set_debug_flags(0, 0)
+        ks = list(range(0, len(tasks), args.serial_every))
+        log(f"plain path one launch at a time over {len(ks)} chromosomes")
+        torch.cuda.synchronize()
+        sev0, sev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        sev0.record(w0["stream"])
+        sst = []
+        for k in ks:
+            t = tasks[k]
+            _, st = w0["eng"].simulate_cells(w0["cids"][k], t["d_seeds"].data_ptr(), t["d_targets"].data_ptr(),
+                                             t["te"], t["nlefs"], t["d_band"].data_ptr(), ncells=len(t["seeds"]))
+            sst += list(st)
+        sev1.record(w0["stream"])
+        torch.cuda.synchronize()
+        sms = sev0.elapsed_time(sev1)
+        btasks_s = [(w0["cids"][k], int(sd), int(tg), tasks[k]["te"], tasks[k]["nlefs"])
+                    for k in ks for sd, tg in zip(tasks[k]["seeds"], tasks[k]["targets"])]
+        log("batched launch over the same chromosomes")
+        bs0, bs1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        bs0.record(w0["stream"])
+        _, bsst = w0["eng"].simulate_batch(btasks_s, {w0["cids"][k]: tasks[k]["d_band"].data_ptr() for k in ks})
+        bs1.record(w0["stream"])
+        torch.cuda.synchronize()
+        bsms = bs0.elapsed_time(bs1)
+        same = all(a.epochs == b.epochs and a.contacts == b.contacts and a.rng_draws == b.rng_draws
+                   for a, b in zip(sst, bsst))
+        serial = {"chromosomes": [tasks[k]["chrom"].name for k in ks], "cells": len(sst), "ms": sms,
+                  "value": sum(x.lef_epochs for x in sst) / (sms / 1e3), "unit": "LEF-epochs/s",
+                  "cells_per_s": len(sst) / (sms / 1e3), "launches": len(ks),
+                  "batched_same_cells": {"ms": bsms, "cells_per_s": len(bsst) / (bsms / 1e3),
+                                         "value": sum(x.lef_epochs for x in bsst) / (bsms / 1e3),
+                                         "per_cell_stats_equal": bool(same)},
+                  "batched_over_serial_cells_per_s": (len(bsst) / bsms) / (len(sst) / sms)}
 
     if rank != 0:
         return
@@ -479,14 +541,32 @@ def run_ours(args):
                                      "launches) x this run's LEF-epochs per launch; alone, a launch's "
                                      "cells stay on chip and in L2, while 24 concurrent launches fill "
                                      "every SM and spill L2 as the batched launch does"},
-        "e2e": e2e, "clocks": clk, "batched": batched,
+        "e2e": e2e, "clocks": clk, "batched": batched, "plain_serial": serial,
     }
+    if batched is not None:
+        line["batched"]["over_plain_wave_cells_per_s"] = batched["cells_per_s"] / line["cells_per_s"]
     if not args.no_cpu_baseline:
         log("cpu baseline")
         threads = os.cpu_count() or 1
         s = cpu_sample_genome(cfg, tasks, args.cpu_seconds, threads)
         line["cpu_baseline"] = {"value": s["lef_epochs"] / s["seconds"], "unit": "LEF-epochs/s",
                                 "cores": threads, "kind": "port", "sample": s["sample"]}
+        # the CPU leg doubles as a parity check: its cells are the GPU's cells of the same ids
+        gpu_cells = {}
+        for k, st, _ in done:
+            if k not in gpu_cells:
+                gpu_cells[k] = st
+        compared = equal = 0
+        for k, cells in s["per_cell"].items():
+            if k not in gpu_cells:
+                continue
+            for (i, ep, ct, dr, le) in cells:
+                g = gpu_cells[k][i]
+                compared += 1
+                equal += int((g.epochs, g.contacts, g.rng_draws, g.lef_epochs) == (ep, ct, dr, le))
+        line["parity"] = {"cells": compared, "equal": equal,
+                          "fields": "epochs, contacts, rng_draws, lef_epochs of each CPU-oracle cell against "
+                                    "the GPU cell of the same chromosome and cell id in the first timed step"}
     print(json.dumps(line), flush=True)
     for w in workers:
         w["eng"].close()

@@ -302,7 +302,8 @@ int mgpu_simulate_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* cell_seeds,
  * global slot per concurrently simulated cell); it takes it from one fixed array of
  * MGPU_NOALLOC_SCRATCH_BYTES that is part of the loaded library, one per device.
  *
- *   - Every buffer must be device memory: cell_seeds, target_contacts and band are required,
+ *   - Every buffer must be device memory of the context's device (or managed memory):
+ *     cell_seeds, target_contacts and band are required,
  *     missed_updates (added to, like mgpu_simulate_cells) and stats may be NULL.
  *   - ncells may be at most MGPU_NOALLOC_MAX_CELLS; larger batches, host pointers and
  *     chromosomes whose global slot does not fit the scratch are rejected with
@@ -311,8 +312,10 @@ int mgpu_simulate_cells(mgpu_ctx* ctx, int chrom_id, const uint64_t* cell_seeds,
  *   - The call only enqueues work on the context's stream and returns; the results are ready
  *     after mgpu_sync (or when the stream completes).  Errors detected on the device (the
  *     per-cell status) are reported through stats[i].status, not through the return value.
- *   - The first call on a device looks up the scratch's address (cudaGetSymbolAddress) with
- *     that device current; make that first call before capturing the stream.
+ *   - The first call on a context looks up the scratch's address (cudaGetSymbolAddress) with
+ *     the context's device current and keeps it with the context; make that first call before
+ *     capturing the stream.  Like every buffer of a context, the address does not survive a
+ *     cudaDeviceReset: destroy the context first and create a new one after the reset.
  *   - The scratch is shared by every context of the process on that device, so calls that
  *     overlap in time (two streams, two contexts, two threads) race on it and give wrong
  *     results: issue them on one stream, or synchronise between them.
@@ -517,6 +520,45 @@ int mgpu_run_phase(mgpu_ctx* ctx, int chrom_id, int phase, mgpu_phase_io* io);
 
 /* Xoshiro256++ seeded through SplitMix64 (random::PRNG, random.hpp:26-30): writes the state. */
 void mgpu_prng_seed(uint64_t seed, uint64_t state[4]);
+
+/*
+ * Probes of the device's floating-point arithmetic (test hooks, no counterpart in the
+ * reference).  The reference computes its transcendentals with the host's libm (glibc); the
+ * device uses CUDA's.  These run the epoch loop's own device code so that the test-suite can
+ * compare it with the host, bit for bit, on the argument streams the loop feeds it.
+ *
+ * mgpu_probe_samplers: per_stream samples from each of nstreams seeded streams (seed as for
+ * mgpu_prng_seed) through the serial samplers the epoch loop uses; out[s * per_stream + i] is
+ * sample i of stream s and draws[s] the raw 64-bit draws stream s consumed (UINT64_MAX if a
+ * sampler hit its iteration limit).  Kinds and parameters:
+ *   MGPU_PROBE_NORMAL              normal(a0, a1): move lengths (simulation.cpp:264-290)
+ *   MGPU_PROBE_EXPONENTIAL         unit exponential (the normal's tail)
+ *   MGPU_PROBE_POISSON             Poisson(a0): burn-in activations (simulation.cpp:1031-1032)
+ *   MGPU_PROBE_BINOMIAL            binomial(a0, a1): loop/TAD split (register_contacts.cpp:73-92)
+ *                                  with (1 - p)^t taken from the host, as in a full epoch
+ *   MGPU_PROBE_BINOMIAL_DEVICE_POW the same with (1 - p)^t evaluated on the device (last epoch)
+ *   MGPU_PROBE_GEV                 genextreme(0, a0, a1) noise (genextreme_value_distribution.hpp:87-105)
+ * mgpu_probe_libm: out[i] = f(x[i], y[i]) on the device for
+ *   MGPU_PROBE_LOG log x, MGPU_PROBE_EXP exp x, MGPU_PROBE_POW pow(x, y),
+ *   MGPU_PROBE_GEV_NOISE the GEV noise of a uniform x with (mu, sigma, xi),
+ *   MGPU_PROBE_BELOW_EXP 1.0 if x < exp(y) as the ziggurat decides it, else 0.0.
+ * Host buffers; the calls allocate and synchronise the device.
+ */
+#define MGPU_PROBE_NORMAL 0
+#define MGPU_PROBE_EXPONENTIAL 1
+#define MGPU_PROBE_POISSON 2
+#define MGPU_PROBE_BINOMIAL 3
+#define MGPU_PROBE_BINOMIAL_DEVICE_POW 4
+#define MGPU_PROBE_GEV 5
+#define MGPU_PROBE_LOG 0
+#define MGPU_PROBE_EXP 1
+#define MGPU_PROBE_POW 2
+#define MGPU_PROBE_GEV_NOISE 3
+#define MGPU_PROBE_BELOW_EXP 4
+int mgpu_probe_samplers(int device, int kind, const uint64_t* seeds, uint64_t nstreams, uint64_t per_stream,
+                        double a0, double a1, double* out, uint64_t* draws);
+int mgpu_probe_libm(int device, int kind, const double* x, const double* y, uint64_t n, double mu,
+                    double sigma, double xi, double* out);
 
 #ifdef __cplusplus
 }

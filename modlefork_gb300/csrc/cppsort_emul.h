@@ -7,6 +7,8 @@
 // partition_right / partition_left, partial insertion sort, heap sort fallback after log2(n)
 // unbalanced partitions) and split_sort (approximate longest ascending subsequence kept on the
 // left, the rest pdq-sorted and merged stably).
+// Algorithms: pdqsort by Orson Peters (zlib licence), as adopted by cpp-sort 1.13 by Morwenn
+// (MIT licence); split_sort of cpp-sort 1.13.  This file restates their published steps.
 #pragma once
 #include "mgpu_internal.h"
 

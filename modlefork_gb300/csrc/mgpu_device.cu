@@ -3283,6 +3283,82 @@ int launch_phase(const KParams& P, const DevChrom& ch, int phase, u64 n, u64* ar
 }
 
 // ---------------------------------------------------------------------------------------
+// Probes of the device's floating-point library (test hooks): the samplers of the epoch loop
+// run on whole seeded streams, and the transcendental functions on caller arguments, so that
+// the test-suite can compare them with the host's libm (glibc, the reference's) bit for bit.
+// ---------------------------------------------------------------------------------------
+
+// One block per stream (grid-stride): lane 0 draws `per` samples of one distribution from the
+// Xoshiro256++ state states[4 s .. 4 s + 3] through the same serial samplers the epoch loop
+// uses, writes them to out[s * per ..] and the number of raw draws taken to draws[s].
+__global__ void __launch_bounds__(32) sampler_probe_kernel(const __grid_constant__ KParams P, int kind,
+                                                           const u64* states, u64 nstreams, u64 per,
+                                                           double a0, double a1, double* out, u64* draws) {
+  __shared__ Scalars sc;
+  __shared__ u64 ring[RING];
+  if (threadIdx.x != 0) return;
+  for (u64 s = blockIdx.x; s < nstreams; s += gridDim.x) {
+    Cell c{};
+    c.sc = &sc;
+    c.ring = ring;
+    sc.rpos = sc.gpos = 0;
+    sc.status = DEV_OK;
+    sc.lanes_stale = 0;
+    sc.prof = nullptr;
+    for (int k = 0; k < 4; ++k) sc.canon[k] = states[4 * s + k];
+    for (u64 i = 0; i < per; ++i) {
+      double v = 0.0;
+      switch (kind) {
+        case 0: v = s_unit_normal(c) * a1 + a0; break;
+        case 1: v = s_unit_exponential(c); break;
+        case 2: v = (double)s_poisson(c, P); break;
+        case 3: v = (double)s_binomial(c, P, (i64)a0, a1); break;
+        case 4: v = s_gev(c, P); break;
+        default: break;
+      }
+      out[s * per + i] = v;
+    }
+    draws[s] = sc.status == DEV_OK ? sc.rpos : ~0ull;
+  }
+}
+
+// out[i] = f(x[i], y[i]) for f = 0: log x, 1: exp x, 2: pow(x, y), 3: the GEV noise of
+// register_contacts.cpp:48-64 from u = x (mu, sigma, xi), 4: below_exp(x, y) as 0 or 1.
+__global__ void libm_probe_kernel(int kind, const double* x, const double* y, u64 n, double mu, double sigma,
+                                  double xi, double* out) {
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
+    const double a = x[i];
+    double r = 0.0;
+    switch (kind) {
+      case 0: r = log(a); break;
+      case 1: r = exp(a); break;
+      case 2: r = pow(a, y[i]); break;
+      case 3: r = xi == 0.0 ? (mu - sigma) * log(-log(a)) : mu + (sigma * (1.0 - pow(-log(a), xi))) / xi; break;
+      case 4: r = below_exp(a, y[i]) ? 1.0 : 0.0; break;
+      default: break;
+    }
+    out[i] = r;
+  }
+}
+
+int launch_sampler_probe(const KParams& P, int kind, const u64* states, u64 nstreams, u64 per, double a0,
+                         double a1, double* out, u64* draws, void* stream, char* errbuf, int errlen) {
+  if (nstreams == 0) return MGPU_OK;
+  const u64 blocks = nstreams < 65535 ? nstreams : 65535;
+  sampler_probe_kernel<<<(unsigned)blocks, 32, 0, (cudaStream_t)stream>>>(P, kind, states, nstreams, per, a0, a1,
+                                                                          out, draws);
+  return cuda_fail(cudaGetLastError(), "sampler_probe_kernel launch", errbuf, errlen);
+}
+
+int launch_libm_probe(int kind, const double* x, const double* y, u64 n, double mu, double sigma, double xi,
+                      double* out, void* stream, char* errbuf, int errlen) {
+  if (n == 0) return MGPU_OK;
+  const u64 blocks = (n + 255) / 256 < 152 * 16 ? (n + 255) / 256 : 152 * 16;
+  libm_probe_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(kind, x, y, n, mu, sigma, xi, out);
+  return cuda_fail(cudaGetLastError(), "libm_probe_kernel launch", errbuf, errlen);
+}
+
+// ---------------------------------------------------------------------------------------
 // Fixed scratch of the allocation-free entry point (one array per device, part of the module)
 // ---------------------------------------------------------------------------------------
 static __device__ __align__(256) unsigned char g_noalloc_scratch[MGPU_NOALLOC_SCRATCH_BYTES];

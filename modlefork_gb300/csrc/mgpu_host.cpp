@@ -564,6 +564,7 @@ struct mgpu_ctx {
   u64 scratch_bytes = 0;
   uint64_t* d_prof = nullptr;  // profile counters of the last launch
   uint64_t h_prof[32] = {0};
+  void* noalloc_scratch = nullptr;  // device address of the fixed scratch, looked up by this context
 };
 
 extern "C" const char* mgpu_last_error_string(void) { return g_last_error.c_str(); }
@@ -875,6 +876,19 @@ static bool is_device_ptr(const void* p) {
     return false;
   }
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Device memory that a kernel on `device` may touch: managed memory, or device memory owned by
+// that device.  Memory of another GPU is refused (its kernels would need peer access).
+static bool is_device_ptr_on(const void* p, int device) {
+  if (!p) return false;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return a.type == cudaMemoryTypeDevice && a.device == device;
 }
 
 // Device buffer (RAII).  Buffers allocated with a stream are stream-ordered
@@ -1275,10 +1289,6 @@ extern "C" int mgpu_band_to_pixels(mgpu_ctx* ctx, const uint32_t* band, uint64_t
   return MGPU_OK;
 }
 
-// Address of the fixed scratch, looked up once per device (with that device current).
-static std::mutex g_noalloc_mu;
-static constexpr int NOALLOC_MAX_DEVICES = 64;
-static void* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
 
 extern "C" int mgpu_simulate_cells_noalloc(mgpu_ctx* ctx, int chrom_id, const uint64_t* cell_seeds,
                                            const uint64_t* target_contacts, uint64_t target_epochs,
@@ -1298,33 +1308,31 @@ extern "C" int mgpu_simulate_cells_noalloc(mgpu_ctx* ctx, int chrom_id, const ui
   const void* need_dev[3] = {cell_seeds, target_contacts, band};
   const char* names[5] = {"cell_seeds", "target_contacts", "band", "missed_updates", "stats"};
   for (int k = 0; k < 3; ++k) {
-    if (!is_device_ptr(need_dev[k]))
-      return fail(MGPU_ERR_INVALID_ARG, "mgpu_simulate_cells_noalloc: %s must be a device pointer", names[k]);
+    if (!is_device_ptr_on(need_dev[k], ctx->device))
+      return fail(MGPU_ERR_INVALID_ARG, "mgpu_simulate_cells_noalloc: %s must be a device pointer of device %d",
+                  names[k], ctx->device);
   }
-  if (missed_updates && !is_device_ptr(missed_updates))
-    return fail(MGPU_ERR_INVALID_ARG, "mgpu_simulate_cells_noalloc: %s must be a device pointer or NULL", names[3]);
-  if (stats && !is_device_ptr(stats))
-    return fail(MGPU_ERR_INVALID_ARG, "mgpu_simulate_cells_noalloc: %s must be a device pointer or NULL", names[4]);
+  if (missed_updates && !is_device_ptr_on(missed_updates, ctx->device))
+    return fail(MGPU_ERR_INVALID_ARG, "mgpu_simulate_cells_noalloc: %s must be a device pointer of device %d or NULL",
+                names[3], ctx->device);
+  if (stats && !is_device_ptr_on(stats, ctx->device))
+    return fail(MGPU_ERR_INVALID_ARG, "mgpu_simulate_cells_noalloc: %s must be a device pointer of device %d or NULL",
+                names[4], ctx->device);
   const ChromEntry& ch = ctx->chroms[chrom_id];
   KParams P;
   int rc = make_kparams(ctx, ch, num_lefs, &P);
   if (rc) return rc;
-  if (ctx->device < 0 || ctx->device >= NOALLOC_MAX_DEVICES)
-    return fail(MGPU_ERR_UNSUPPORTED, "mgpu_simulate_cells_noalloc: device %d out of range", ctx->device);
   char err[256] = {0};
-  void* base = nullptr;
-  {
-    std::lock_guard<std::mutex> g(g_noalloc_mu);
-    if (!g_noalloc_addr[ctx->device]) {
-      rc = noalloc_scratch_address(&g_noalloc_addr[ctx->device], err, sizeof(err));
-      if (rc) {
-        g_noalloc_addr[ctx->device] = nullptr;
-        return fail(rc, "%s", err);
-      }
-    }
-    base = g_noalloc_addr[ctx->device];
+  // The array's address in the CUDA context current on ctx->device, looked up on this mgpu
+  // context's first call and kept with the context (whose own device buffers belong to the same
+  // CUDA context and die with it).
+  if (!ctx->noalloc_scratch) {
+    void* addr = nullptr;
+    rc = noalloc_scratch_address(&addr, err, sizeof(err));
+    if (rc) return fail(rc, "%s", err);
+    ctx->noalloc_scratch = addr;
   }
-  char* scratch = (char*)base;
+  char* scratch = (char*)ctx->noalloc_scratch;
   const u64 slot_room = MGPU_NOALLOC_SCRATCH_BYTES - NOALLOC_SLOTS_OFFSET;
   if (P.slot_bytes > slot_room)
     return fail(MGPU_ERR_UNSUPPORTED,
@@ -1509,4 +1517,98 @@ extern "C" int mgpu_run_phase(mgpu_ctx* ctx, int chrom_id, int phase, mgpu_phase
     return status_from_stats(&s, 1);
   }
   return MGPU_OK;
+}
+
+// ===========================================================================================
+// Probes of the device's floating-point library (test hooks, no reference counterpart)
+// ===========================================================================================
+extern "C" int mgpu_probe_samplers(int device, int kind, const uint64_t* seeds, uint64_t nstreams,
+                                   uint64_t per_stream, double a0, double a1, double* out, uint64_t* draws) {
+  if ((nstreams && (!seeds || !out || !draws)) || kind < 0 || kind > MGPU_PROBE_GEV)
+    return fail(MGPU_ERR_INVALID_ARG, "mgpu_probe_samplers: bad argument");
+  if (nstreams == 0 || per_stream == 0) return MGPU_OK;
+  CK(cudaSetDevice(device));
+  KParams P{};
+  int dev_kind = 0;
+  switch (kind) {
+    case MGPU_PROBE_NORMAL: dev_kind = 0; break;
+    case MGPU_PROBE_EXPONENTIAL: dev_kind = 1; break;
+    case MGPU_PROBE_POISSON: {
+      // constants as the epoch loop's burn-in Poisson has them (make_kparams)
+      dev_kind = 2;
+      const double mean = a0;
+      P.pois_mean = mean;
+      P.pois_exp_mean = std::exp(-mean);
+      P.pois_smu = std::sqrt(mean);
+      P.pois_b = 0.931 + 2.53 * P.pois_smu;
+      P.pois_a = -0.059 + 0.02483 * P.pois_b;
+      P.pois_inv_alpha = 1.1239 + 1.1328 / (P.pois_b - 3.4);
+      P.pois_v_r = 0.9277 - 3.6224 / (P.pois_b - 2);
+      break;
+    }
+    case MGPU_PROBE_BINOMIAL:
+    case MGPU_PROBE_BINOMIAL_DEVICE_POW: {
+      dev_kind = 3;
+      const double p = (0.5 < a1) ? (1 - a1) : a1;
+      // the epoch loop's full epochs take (1 - p)^t from the host; a last, shorter epoch
+      // evaluates it on the device
+      P.spe = kind == MGPU_PROBE_BINOMIAL ? (uint64_t)(int64_t)a0 : ~0ull;
+      P.bin_q_n = std::pow((1 - p), (double)(int64_t)a0);
+      break;
+    }
+    case MGPU_PROBE_GEV:
+      dev_kind = 4;
+      P.gev_mu = 0.0;
+      P.gev_sigma = a0;
+      P.gev_xi = a1;
+      break;
+  }
+  std::vector<uint64_t> states(4 * nstreams);
+  for (uint64_t s = 0; s < nstreams; ++s) mgpu_prng_seed(seeds[s], &states[4 * s]);
+  u64 *d_states = nullptr, *d_draws = nullptr;
+  double* d_out = nullptr;
+  const size_t nout = (size_t)nstreams * per_stream;
+  int rc = cuda_check(cudaMalloc(&d_states, states.size() * 8), "cudaMalloc(states)");
+  if (!rc) rc = cuda_check(cudaMalloc(&d_out, nout * 8), "cudaMalloc(samples)");
+  if (!rc) rc = cuda_check(cudaMalloc(&d_draws, nstreams * 8), "cudaMalloc(draws)");
+  if (!rc) rc = cuda_check(cudaMemcpy(d_states, states.data(), states.size() * 8, cudaMemcpyHostToDevice), "copy");
+  char err[256] = {0};
+  if (!rc) {
+    rc = launch_sampler_probe(P, dev_kind, d_states, nstreams, per_stream, a0, a1, d_out, d_draws, nullptr, err,
+                              sizeof(err));
+    if (rc) rc = fail(rc, "%s", err);
+  }
+  if (!rc) rc = cuda_check(cudaDeviceSynchronize(), "sampler probe");
+  if (!rc) rc = cuda_check(cudaMemcpy(out, d_out, nout * 8, cudaMemcpyDeviceToHost), "copy samples");
+  if (!rc) rc = cuda_check(cudaMemcpy(draws, d_draws, nstreams * 8, cudaMemcpyDeviceToHost), "copy draws");
+  cudaFree(d_states);
+  cudaFree(d_out);
+  cudaFree(d_draws);
+  return rc;
+}
+
+extern "C" int mgpu_probe_libm(int device, int kind, const double* x, const double* y, uint64_t n, double mu,
+                               double sigma, double xi, double* out) {
+  const bool needs_y = kind == MGPU_PROBE_POW || kind == MGPU_PROBE_BELOW_EXP;
+  if ((n && (!x || !out || (needs_y && !y))) || kind < 0 || kind > MGPU_PROBE_BELOW_EXP)
+    return fail(MGPU_ERR_INVALID_ARG, "mgpu_probe_libm: bad argument");
+  if (n == 0) return MGPU_OK;
+  CK(cudaSetDevice(device));
+  double *d_x = nullptr, *d_y = nullptr, *d_out = nullptr;
+  int rc = cuda_check(cudaMalloc(&d_x, n * 8), "cudaMalloc(x)");
+  if (!rc && needs_y) rc = cuda_check(cudaMalloc(&d_y, n * 8), "cudaMalloc(y)");
+  if (!rc) rc = cuda_check(cudaMalloc(&d_out, n * 8), "cudaMalloc(out)");
+  if (!rc) rc = cuda_check(cudaMemcpy(d_x, x, n * 8, cudaMemcpyHostToDevice), "copy x");
+  if (!rc && needs_y) rc = cuda_check(cudaMemcpy(d_y, y, n * 8, cudaMemcpyHostToDevice), "copy y");
+  char err[256] = {0};
+  if (!rc) {
+    rc = launch_libm_probe(kind, d_x, d_y, n, mu, sigma, xi, d_out, nullptr, err, sizeof(err));
+    if (rc) rc = fail(rc, "%s", err);
+  }
+  if (!rc) rc = cuda_check(cudaDeviceSynchronize(), "libm probe");
+  if (!rc) rc = cuda_check(cudaMemcpy(out, d_out, n * 8, cudaMemcpyDeviceToHost), "copy out");
+  cudaFree(d_x);
+  cudaFree(d_y);
+  cudaFree(d_out);
+  return rc;
 }

@@ -222,6 +222,14 @@ int launch_band_counts(const u32* band, u64 nrows, u64 ncols, u32* counts, u64* 
 int launch_band_pixels(const u32* band, u64 nrows, u64 ncols, u64 bin_offset, const u64* offsets,
                        int64_t* bin1, int64_t* bin2, u32* count, void* stream, char* errbuf, int errlen);
 
+// Test hooks: the epoch loop's serial samplers on seeded streams (kind 0 normal(a0, a1),
+// 1 unit exponential, 2 Poisson(P.pois_*), 3 binomial(a0, a1) with P.spe / P.bin_q_n, 4 GEV
+// with P.gev_*) and the device's log / exp / pow / GEV noise / below_exp on arguments.
+int launch_sampler_probe(const KParams& P, int kind, const u64* states, u64 nstreams, u64 per, double a0,
+                         double a1, double* out, u64* draws, void* stream, char* errbuf, int errlen);
+int launch_libm_probe(int kind, const double* x, const double* y, u64 n, double mu, double sigma, double xi,
+                      double* out, void* stream, char* errbuf, int errlen);
+
 // Address of the scratch on the current device.
 int noalloc_scratch_address(void** ptr, char* errbuf, int errlen);
 // tasks[i] = {seeds[i], targets[i]} on the stream.

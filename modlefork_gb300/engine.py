@@ -76,6 +76,10 @@ def load(path=LIB_PATH):
         "mgpu_last_kernel_ms": (i32, [C.c_void_p, P(C.c_double)]),
         "mgpu_set_debug_flags": (i32, [C.c_void_p, C.c_uint32, u64]),
         "mgpu_last_profile": (i32, [C.c_void_p, P(u64)]),
+        "mgpu_probe_samplers": (i32, [i32, i32, C.c_void_p, u64, u64, C.c_double, C.c_double, C.c_void_p,
+                                      C.c_void_p]),
+        "mgpu_probe_libm": (i32, [i32, i32, C.c_void_p, C.c_void_p, u64, C.c_double, C.c_double, C.c_double,
+                                  C.c_void_p]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(lib, name)
@@ -150,6 +154,35 @@ def barriers_from_bed(chrom, records, default_stp_active, default_stp_inactive):
         if rc == 1:
             out.append(dict(pos=b.pos, stp_active=b.stp_active, stp_inactive=b.stp_inactive,
                             blocking_dir=b.blocking_dir))
+    return out
+
+
+PROBE_NORMAL, PROBE_EXPONENTIAL, PROBE_POISSON, PROBE_BINOMIAL, PROBE_BINOMIAL_DEVICE_POW, PROBE_GEV = range(6)
+PROBE_LOG, PROBE_EXP, PROBE_POW, PROBE_GEV_NOISE, PROBE_BELOW_EXP = range(5)
+
+
+def probe_samplers(kind, seeds, per_stream, a0=0.0, a1=0.0, device=0):
+    """The epoch loop's serial samplers on the device (test hook mgpu_probe_samplers):
+    (samples[nstreams, per_stream], draws[nstreams])."""
+    seeds = np.ascontiguousarray(seeds, dtype=np.uint64)
+    out = np.empty((len(seeds), per_stream), dtype=np.float64)
+    draws = np.empty(len(seeds), dtype=np.uint64)
+    _check(load().mgpu_probe_samplers(device, kind, seeds.ctypes.data, len(seeds), per_stream, a0, a1,
+                                      out.ctypes.data, draws.ctypes.data), "mgpu_probe_samplers")
+    return out, draws
+
+
+def probe_libm(kind, x, y=None, mu=0.0, sigma=0.0, xi=0.0, device=0):
+    """The device's log / exp / pow / GEV noise / below_exp on arguments (test hook
+    mgpu_probe_libm)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    yp = None
+    if y is not None:
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        yp = y.ctypes.data
+    out = np.empty_like(x)
+    _check(load().mgpu_probe_libm(device, kind, x.ctypes.data, yp, len(x), mu, sigma, xi, out.ctypes.data),
+           "mgpu_probe_libm")
     return out
 
 

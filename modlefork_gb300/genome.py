@@ -18,6 +18,10 @@ parity and genome-scale workloads:
 Barriers are produced as BED records [p, p + 1) (so the reference's midpoint rule
 (start + end + 1) / 2 of genome.cpp:199 puts the barrier at p + 1) in IITree order (sorted by
 start, distinct positions), then converted with mgpu_barrier_from_bed.
+
+Every generator takes ``api``: the module or object answering config_defaults,
+config_transform, Chromosome and barriers_from_bed (the engine by default).  The CPU arm of the
+benchmark passes the oracle's helpers instead, so that it never loads the product library.
 """
 
 import numpy as np
@@ -41,9 +45,10 @@ def bed_records(rng, length, nbarriers, occupancy=None):
     return [(int(s), int(s) + 1, str(st), float(sc)) for s, st, sc in zip(starts, strands, scores)]
 
 
-def parity_config(**overrides):
+def parity_config(api=None, **overrides):
     """Transformed Config of the 10 Mbp parity workload."""
-    cfg = engine.config_defaults(
+    api = api or engine
+    cfg = api.config_defaults(
         bin_size=5000, diagonal_width=3_000_000, rev_extrusion_speed=2500, fwd_extrusion_speed=2500,
         rev_speed_set=1, fwd_speed_set=1, rev_extrusion_speed_std=0.05, fwd_extrusion_speed_std=0.05,
         number_of_lefs_per_mbp=20.0, avg_lef_processivity=200_000, barrier_occupied_stp=0.7,
@@ -51,46 +56,51 @@ def parity_config(**overrides):
         seed=20231203, target_contact_density=1.0)
     for k, v in overrides.items():
         setattr(cfg, k, v)
-    return engine.config_transform(cfg)
+    return api.config_transform(cfg)
 
 
-def parity_10mbp(seed=7, **overrides):
-    cfg = parity_config(**overrides)
+def parity_10mbp(seed=7, api=None, **overrides):
+    api = api or engine
+    cfg = parity_config(api=api, **overrides)
     rng = np.random.default_rng(seed)
-    chrom = engine.Chromosome("chrS", 10_000_000)
+    chrom = api.Chromosome("chrS", 10_000_000)
     recs = bed_records(rng, chrom.size, 100)
-    bars = engine.barriers_from_bed(chrom, recs, cfg.barrier_occupied_stp, cfg.barrier_not_occupied_stp)
+    bars = api.barriers_from_bed(chrom, recs, cfg.barrier_occupied_stp, cfg.barrier_not_occupied_stp)
     return cfg, [(chrom, bars)]
 
 
-def genome_config(**overrides):
+def genome_config(api=None, **overrides):
     """Transformed Config of the genome-scale workload (defaults except lifetime, 512 cells)."""
-    cfg = engine.config_defaults(bin_size=5000, diagonal_width=3_000_000, number_of_lefs_per_mbp=20.0,
-                                 avg_lef_processivity=200_000, num_cells=512, seed=20231203,
-                                 target_contact_density=1.0)
+    api = api or engine
+    cfg = api.config_defaults(bin_size=5000, diagonal_width=3_000_000, number_of_lefs_per_mbp=20.0,
+                              avg_lef_processivity=200_000, num_cells=512, seed=20231203,
+                              target_contact_density=1.0)
     for k, v in overrides.items():
         setattr(cfg, k, v)
-    return engine.config_transform(cfg)
+    return api.config_transform(cfg)
 
 
-def genome_24chr(seed=11, nchroms=24, min_len=50_000_000, max_len=250_000_000, **overrides):
-    cfg = genome_config(**overrides)
+def genome_24chr(seed=11, nchroms=24, min_len=50_000_000, max_len=250_000_000, api=None, **overrides):
+    api = api or engine
+    cfg = genome_config(api=api, **overrides)
     rng = np.random.default_rng(seed)
     lengths = rng.integers(min_len, max_len + 1, size=nchroms)
     out = []
     for k, L in enumerate(lengths):
-        chrom = engine.Chromosome(f"chr{k + 1}", int(L))
+        chrom = api.Chromosome(f"chr{k + 1}", int(L))
         nb = int(round(L / 50_000))
         occ = rng.beta(8.0, 2.0, size=nb)
         recs = bed_records(rng, int(L), nb, occ)
-        bars = engine.barriers_from_bed(chrom, recs, cfg.barrier_occupied_stp, cfg.barrier_not_occupied_stp)
+        bars = api.barriers_from_bed(chrom, recs, cfg.barrier_occupied_stp, cfg.barrier_not_occupied_stp)
         out.append((chrom, bars))
     return cfg, out
 
 
-def batched_windows(seed=13, nwindows=4096, min_len=1_000_000, max_len=250_000_000, cells=256, **overrides):
+def batched_windows(seed=13, nwindows=4096, min_len=1_000_000, max_len=250_000_000, cells=256, api=None,
+                    **overrides):
     """Windows of the batched workload, each a sequence of its own with its own transformed
     configuration; returns a list of (cfg, chrom, barriers)."""
+    api = api or engine
     rng = np.random.default_rng(seed)
     out = []
     for k in range(nwindows):
@@ -98,12 +108,12 @@ def batched_windows(seed=13, nwindows=4096, min_len=1_000_000, max_len=250_000_0
         bin_size = 1000 * int(rng.integers(1, 11))
         lef_density = float(rng.uniform(5.0, 40.0))
         bar_density = float(rng.uniform(5.0, 40.0))
-        cfg = genome_config(bin_size=bin_size, number_of_lefs_per_mbp=lef_density, num_cells=cells,
+        cfg = genome_config(api=api, bin_size=bin_size, number_of_lefs_per_mbp=lef_density, num_cells=cells,
                             **overrides)
-        chrom = engine.Chromosome(f"win{k + 1}", L)
+        chrom = api.Chromosome(f"win{k + 1}", L)
         nb = int(round(L / 1e6 * bar_density))
         occ = rng.beta(8.0, 2.0, size=nb)
         recs = bed_records(rng, L, nb, occ)
-        bars = engine.barriers_from_bed(chrom, recs, cfg.barrier_occupied_stp, cfg.barrier_not_occupied_stp)
+        bars = api.barriers_from_bed(chrom, recs, cfg.barrier_occupied_stp, cfg.barrier_not_occupied_stp)
         out.append((cfg, chrom, bars))
     return out

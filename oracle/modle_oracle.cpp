@@ -50,6 +50,11 @@ using bp_t = uint64_t;
 static constexpr u64 U64MAX = std::numeric_limits<u64>::max();
 static constexpr double TWO64 = 18446744073709551616.0;
 
+// Full-tie counters of rank_lefs (off unless orc_tie_counters enables them, so that the timed
+// CPU baseline runs the reference's work only).
+static std::atomic<bool> g_count_ties{false};
+static std::atomic<u64> g_tie_rank_calls{0}, g_tie_calls{0}, g_tie_pairs{0}, g_tie_interior{0};
+
 // ---------------------------------------------------------------------------------------
 // PRNG: random::PRNG (src/common/include/modle/common/random.hpp:26-30)
 // ---------------------------------------------------------------------------------------
@@ -803,6 +808,7 @@ struct Sim {
       if (!mask || mask[i]) lefs[i].bind(epoch, uniform_int(g, start, end - 1));
     }
     rank_lefs(lefs, n, rr, fr, epoch != 0, false);
+    if (g_count_ties.load(std::memory_order_relaxed)) count_full_ties(lefs, n, rr, fr, start, end);
   }
 
   // rank_lefs (simulation.cpp:402-487)
@@ -845,6 +851,36 @@ struct Sim {
           return lefs[b].binding_epoch < lefs[a].binding_epoch;
         });
       }
+    }
+  }
+
+  // Full ties: neighbours in a rank order that are bound and share both the position and the
+  // binding epoch.  Their relative order is whatever the sort's element moves leave, the one
+  // part of the ranking the reference's tests do not pin (cpp-sort's unstable sorts).  Ties of
+  // units parked at a chromosome end (rev at start, fwd at end - 1) are counted apart from
+  // interior ones.
+  static void count_full_ties(const std::vector<Lef>& lefs, usize n, const std::vector<usize>& rr,
+                              const std::vector<usize>& fr, bp_t start, bp_t end) {
+    u64 pairs = 0, interior = 0;
+    for (usize i = 1; i < n; ++i) {
+      const Lef& a = lefs[rr[i - 1]];
+      const Lef& b = lefs[rr[i]];
+      if (a.bound() && b.bound() && a.rev == b.rev && a.binding_epoch == b.binding_epoch) {
+        ++pairs;
+        interior += a.rev != start;
+      }
+      const Lef& c = lefs[fr[i - 1]];
+      const Lef& d = lefs[fr[i]];
+      if (c.bound() && d.bound() && c.fwd == d.fwd && c.binding_epoch == d.binding_epoch) {
+        ++pairs;
+        interior += c.fwd != end - 1;
+      }
+    }
+    g_tie_rank_calls.fetch_add(1, std::memory_order_relaxed);
+    if (pairs) {
+      g_tie_calls.fetch_add(1, std::memory_order_relaxed);
+      g_tie_pairs.fetch_add(pairs, std::memory_order_relaxed);
+      g_tie_interior.fetch_add(interior, std::memory_order_relaxed);
     }
   }
 
@@ -2108,6 +2144,252 @@ int orc_band_to_pixels(const uint32_t* band, uint64_t nrows, uint64_t ncols, uin
   bin1_offset[ncols] = k;
   *nnz = k;
   return k <= capacity ? MGPU_OK : MGPU_ERR_OVERFLOW;
+}
+
+
+// Full-tie counters of the epoch loop's rank_lefs calls: enable (1) or disable (0) counting,
+// optionally reset, and read out[0] = rank_lefs calls counted, out[1] = calls with at least one
+// full tie, out[2] = adjacent full-tie pairs (rev and fwd orders together), out[3] = those of
+// out[2] away from the chromosome ends.
+void orc_tie_counters(int enable, int reset, uint64_t out[4]) {
+  if (reset) {
+    g_tie_rank_calls = 0;
+    g_tie_calls = 0;
+    g_tie_pairs = 0;
+    g_tie_interior = 0;
+  }
+  g_count_ties = enable != 0;
+  if (out) {
+    out[0] = g_tie_rank_calls.load();
+    out[1] = g_tie_calls.load();
+    out[2] = g_tie_pairs.load();
+    out[3] = g_tie_interior.load();
+  }
+}
+
+// Band shape of ContactMatrixDense(length, diagonal_width, bin_size)
+// (src/contact_matrix/contact_matrix_dense_impl.hpp:40-51) and Chromosome::npixels
+// (src/libmodle/internal/genome_impl.hpp:20-25).
+void orc_band_shape(const mgpu_config* c, uint64_t size_bp, uint64_t* nrows, uint64_t* ncols) {
+  const u64 bins = (size_bp + c->bin_size - 1) / c->bin_size;
+  const u64 diag = (c->diagonal_width + c->bin_size - 1) / c->bin_size;
+  *nrows = diag < bins ? diag : bins;
+  *ncols = bins;
+}
+
+// Chromosome::add_extrusion_barrier (src/libmodle/internal/genome.cpp:194-210) with
+// compute_barrier_stp (genome.cpp:181-192) and ExtrusionBarrier's motif-to-blocking-direction
+// rule (extrusion_barriers_impl.hpp:48-72): the barrier sits at the BED interval's midpoint
+// (start + end + 1) / 2; a non-zero score is the occupancy, from which stp_active follows
+// (compute_stp_active_from_occupancy, extrusion_barriers_impl.hpp:106-116); strand '+' blocks
+// reverse units.  Returns 1 and fills *out for a barrier inside [chrom->start, chrom->end),
+// 0 for one outside it, MGPU_ERR_INVALID_ARG for a bad strand.
+int orc_barrier_from_bed(const mgpu_chrom* chrom, uint64_t bed_start, uint64_t bed_end, char strand,
+                         double score, double stp_active_default, double stp_inactive_default,
+                         mgpu_barrier* out) {
+  if (strand != '+' && strand != '-') return MGPU_ERR_INVALID_ARG;
+  const u64 mid = (bed_start + bed_end + 1) / 2;
+  if (mid < chrom->start || mid >= chrom->end) return 0;
+  double active = stp_active_default;
+  if (score != 0.0) {
+    const double free_to_bound = 1.0 - stp_inactive_default;
+    const double bound_to_free = (free_to_bound - (score * free_to_bound)) / score;
+    active = std::clamp(1.0 - bound_to_free, 0.0, 1.0);
+  }
+  *out = mgpu_barrier{};
+  out->pos = mid;
+  out->stp_active = active;
+  out->stp_inactive = stp_inactive_default;
+  out->blocking_dir = strand == '+' ? MGPU_DIR_REV : MGPU_DIR_FWD;
+  return 1;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// XXH3-64 with a seed, for Chromosome::hash (src/libmodle/internal/genome.cpp:317-335).
+// xxHash 0.8.1 is a dependency the reference does not vendor; this restates the published
+// XXH3 specification (doc/xxhash_spec.md of the xxHash project) for inputs of at most 240
+// bytes, the only lengths a chromosome name plus two 64-bit words reach.  It is written
+// independently of the product's own hash so that the CPU arm derives its seeds without the
+// product library.
+// ---------------------------------------------------------------------------------------
+namespace orc_xxh3 {
+// The 192-byte default secret of the specification.
+static const u8 kDefaultSecret[192] = {
+    0xb8, 0xfe, 0x6c, 0x39, 0x23, 0xa4, 0x4b, 0xbe, 0x7c, 0x01, 0x81, 0x2c, 0xf7, 0x21, 0xad, 0x1c,
+    0xde, 0xd4, 0x6d, 0xe9, 0x83, 0x90, 0x97, 0xdb, 0x72, 0x40, 0xa4, 0xa4, 0xb7, 0xb3, 0x67, 0x1f,
+    0xcb, 0x79, 0xe6, 0x4e, 0xcc, 0xc0, 0xe5, 0x78, 0x82, 0x5a, 0xd0, 0x7d, 0xcc, 0xff, 0x72, 0x21,
+    0xb8, 0x08, 0x46, 0x74, 0xf7, 0x43, 0x24, 0x8e, 0xe0, 0x35, 0x90, 0xe6, 0x81, 0x3a, 0x26, 0x4c,
+    0x3c, 0x28, 0x52, 0xbb, 0x91, 0xc3, 0x00, 0xcb, 0x88, 0xd0, 0x65, 0x8b, 0x1b, 0x53, 0x2e, 0xa3,
+    0x71, 0x64, 0x48, 0x97, 0xa2, 0x0d, 0xf9, 0x4e, 0x38, 0x19, 0xef, 0x46, 0xa9, 0xde, 0xac, 0xd8,
+    0xa8, 0xfa, 0x76, 0x3f, 0xe3, 0x9c, 0x34, 0x3f, 0xf9, 0xdc, 0xbb, 0xc7, 0xc7, 0x0b, 0x4f, 0x1d,
+    0x8a, 0x51, 0xe0, 0x4b, 0xcd, 0xb4, 0x59, 0x31, 0xc8, 0x9f, 0x7e, 0xc9, 0xd9, 0x78, 0x73, 0x64,
+    0xea, 0xc5, 0xac, 0x83, 0x34, 0xd3, 0xeb, 0xc3, 0xc5, 0x81, 0xa0, 0xff, 0xfa, 0x13, 0x63, 0xeb,
+    0x17, 0x0d, 0xdd, 0x51, 0xb7, 0xf0, 0xda, 0x49, 0xd3, 0x16, 0x55, 0x26, 0x29, 0xd4, 0x68, 0x9e,
+    0x2b, 0x16, 0xbe, 0x58, 0x7d, 0x47, 0xa1, 0xfc, 0x8f, 0xf8, 0xb8, 0xd1, 0x7a, 0xd0, 0x31, 0xce,
+    0x45, 0xcb, 0x3a, 0x8f, 0x95, 0x16, 0x04, 0x28, 0xaf, 0xd7, 0xfb, 0xca, 0xbb, 0x4b, 0x40, 0x7e,
+};
+static const u64 kPrime32[3] = {0x9E3779B1ull, 0x85EBCA77ull, 0xC2B2AE3Dull};
+static const u64 kPrime64[5] = {0x9E3779B185EBCA87ull, 0xC2B2AE3D27D4EB4Full, 0x165667B19E3779F9ull,
+                                0x85EBCA77C2B2AE63ull, 0x27D4EB2F165667C5ull};
+
+// Little-endian reads of k bytes, independent of the host's byte order.
+static u64 le(const u8* p, int k) {
+  u64 v = 0;
+  for (int i = 0; i < k; ++i) v |= static_cast<u64>(p[i]) << (8 * i);
+  return v;
+}
+static u64 rotl64(u64 x, unsigned r) { return (x << r) | (x >> (64 - r)); }
+// Byte reversal of the low 32 bits.
+static u64 swap32(u64 x) {
+  return ((x & 0xffu) << 24) | ((x & 0xff00u) << 8) | ((x >> 8) & 0xff00u) | ((x >> 24) & 0xffu);
+}
+static u64 swap64(u64 x) {
+  u64 r = 0;
+  for (int i = 0; i < 8; ++i, x >>= 8) r = (r << 8) | (x & 0xffu);
+  return r;
+}
+// 64x64 -> 128-bit product, folded by xor of its halves.
+static u64 fold_mul(u64 a, u64 b) {
+  const unsigned __int128 m = static_cast<unsigned __int128>(a) * b;
+  return static_cast<u64>(m) ^ static_cast<u64>(m >> 64);
+}
+static u64 avalanche_xxh64(u64 h) {
+  h = (h ^ (h >> 33)) * kPrime64[1];
+  h = (h ^ (h >> 29)) * kPrime64[2];
+  return h ^ (h >> 32);
+}
+static u64 avalanche_xxh3(u64 h) {
+  h = (h ^ (h >> 37)) * 0x165667919E3779F9ull;
+  return h ^ (h >> 32);
+}
+// One 16-byte lane of input against 16 bytes of secret.
+static u64 lane16(const u8* in, const u8* sec, u64 seed) {
+  const u64 lo = le(in, 8) ^ (le(sec, 8) + seed);
+  const u64 hi = le(in + 8, 8) ^ (le(sec + 8, 8) - seed);
+  return fold_mul(lo, hi);
+}
+
+static bool hash64(const u8* in, u64 n, u64 seed, u64* out) {
+  const u8* sec = kDefaultSecret;
+  if (n == 0) {
+    *out = avalanche_xxh64(seed ^ le(sec + 56, 8) ^ le(sec + 64, 8));
+  } else if (n < 4) {
+    const u64 word = (static_cast<u64>(in[0]) << 16) | (static_cast<u64>(in[n / 2]) << 24) |
+                     static_cast<u64>(in[n - 1]) | (n << 8);
+    const u64 key = (le(sec, 4) ^ le(sec + 4, 4)) + seed;
+    *out = avalanche_xxh64(word ^ key);
+  } else if (n <= 8) {
+    const u64 s2 = seed ^ (swap32(seed & 0xffffffffu) << 32);
+    const u64 key = (le(sec + 8, 8) ^ le(sec + 16, 8)) - s2;
+    const u64 v = le(in + n - 4, 4) + (le(in, 4) << 32);
+    u64 h = v ^ key;
+    h ^= rotl64(h, 49) ^ rotl64(h, 24);
+    h *= 0x9FB21C651E98DF25ull;
+    h ^= (h >> 35) + n;
+    h *= 0x9FB21C651E98DF25ull;
+    *out = h ^ (h >> 28);
+  } else if (n <= 16) {
+    const u64 lo = le(in, 8) ^ ((le(sec + 24, 8) ^ le(sec + 32, 8)) + seed);
+    const u64 hi = le(in + n - 8, 8) ^ ((le(sec + 40, 8) ^ le(sec + 48, 8)) - seed);
+    *out = avalanche_xxh3(n + swap64(lo) + hi + fold_mul(lo, hi));
+  } else if (n <= 128) {
+    // Pairs of lanes taken from both ends inwards: pair k reads bytes [16k, 16k + 16) and
+    // [n - 16(k + 1), n - 16k) against secret bytes [32k, 32k + 32).
+    u64 acc = n * kPrime64[0];
+    const u64 pairs = (n - 1) / 32 + 1;
+    for (u64 k = 0; k < pairs; ++k) {
+      acc += lane16(in + 16 * k, sec + 32 * k, seed);
+      acc += lane16(in + n - 16 * (k + 1), sec + 32 * k + 16, seed);
+    }
+    *out = avalanche_xxh3(acc);
+  } else if (n <= 240) {
+    u64 acc = n * kPrime64[0];
+    for (u64 k = 0; k < 8; ++k) acc += lane16(in + 16 * k, sec + 16 * k, seed);
+    acc = avalanche_xxh3(acc);
+    for (u64 k = 8; k < n / 16; ++k) acc += lane16(in + 16 * k, sec + 16 * (k - 8) + 3, seed);
+    acc += lane16(in + n - 16, sec + 136 - 17, seed);
+    *out = avalanche_xxh3(acc);
+  } else {
+    return false;
+  }
+  return true;
+}
+}  // namespace orc_xxh3
+
+extern "C" {
+
+// The host libm (glibc, as the reference links it) on arguments: out[i] = f(x[i], y[i]) with
+// the kinds of the device probe: 0 log x, 1 exp x, 2 pow(x, y), 3 the GEV noise of a uniform x
+// (genextreme_value_distribution.hpp:87-105) with (mu, sigma, xi), 4 x < exp(y) as 1.0 / 0.0.
+// Threads split the range.
+int orc_libm_eval(int kind, const double* x, const double* y, uint64_t n, double mu, double sigma, double xi,
+                  double* out, uint64_t nthreads) {
+  if (kind < 0 || kind > 4) return MGPU_ERR_INVALID_ARG;
+  auto work = [&](u64 lo, u64 hi) {
+    for (u64 i = lo; i < hi; ++i) {
+      const double a = x[i];
+      double r = 0.0;
+      switch (kind) {
+        case 0: r = std::log(a); break;
+        case 1: r = std::exp(a); break;
+        case 2: r = std::pow(a, y[i]); break;
+        case 3:
+          r = xi == 0.0 ? (mu - sigma) * std::log(-std::log(a))
+                        : mu + (sigma * (1.0 - std::pow(-std::log(a), xi))) / xi;
+          break;
+        case 4: r = a < std::exp(y[i]) ? 1.0 : 0.0; break;
+      }
+      out[i] = r;
+    }
+  };
+  const u64 nt = std::max<u64>(1, std::min<u64>(nthreads, n / 4096 + 1));
+  std::vector<std::thread> pool;
+  for (u64 t = 0; t < nt; ++t) pool.emplace_back(work, n * t / nt, n * (t + 1) / nt);
+  for (auto& t : pool) t.join();
+  return MGPU_OK;
+}
+
+// orc_sample over many streams in parallel: per_stream samples of one kind from each seed
+// (out[s * per_stream + i]), draws[s] = raw draws stream s took.
+int orc_sample_streams(const uint64_t* seeds, uint64_t nstreams, uint64_t per_stream, int kind, uint64_t a,
+                       uint64_t b, double p, double q, double* out, uint64_t* draws, uint64_t nthreads) {
+  std::atomic<u64> next{0};
+  auto work = [&]() {
+    for (;;) {
+      const u64 s = next.fetch_add(1);
+      if (s >= nstreams) return;
+      draws[s] = orc_sample(seeds[s], kind, a, b, p, q, per_stream, out + s * per_stream);
+    }
+  };
+  std::vector<std::thread> pool;
+  for (u64 t = 0; t < std::max<u64>(1, nthreads); ++t) pool.emplace_back(work);
+  for (auto& t : pool) t.join();
+  return MGPU_OK;
+}
+
+// XXH3_64bits_withSeed for inputs of at most 240 bytes (0 with *ok = 0 beyond).
+uint64_t orc_xxh3_64(const void* data, uint64_t len, uint64_t seed, int* ok) {
+  u64 h = 0;
+  const bool good = orc_xxh3::hash64(static_cast<const u8*>(data), len, seed, &h);
+  if (ok) *ok = good ? 1 : 0;
+  return h;
+}
+
+// Chromosome::hash (genome.cpp:317-335): XXH3 with Config::seed over the name's bytes, the
+// chromosome size and the cell id (both 64-bit little-endian).
+uint64_t orc_cell_seed(const char* name, uint64_t name_len, uint64_t chrom_size, uint64_t seed,
+                       uint64_t cell_id) {
+  std::vector<u8> msg(name_len + 16);
+  std::memcpy(msg.data(), name, name_len);
+  for (int i = 0; i < 8; ++i) {
+    msg[name_len + i] = static_cast<u8>(chrom_size >> (8 * i));
+    msg[name_len + 8 + i] = static_cast<u8>(cell_id >> (8 * i));
+  }
+  u64 h = 0;
+  orc_xxh3::hash64(msg.data(), msg.size(), seed, &h);
+  return h;
 }
 
 }  // extern "C"

@@ -72,8 +72,98 @@ def load_oracle():
     lib.orc_band_to_pixels.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, P(C.c_uint64)]
     lib.orc_band_to_pixels.restype = C.c_int
+    lib.orc_tie_counters.argtypes = [C.c_int, C.c_int, P(C.c_uint64)]
+    lib.orc_tie_counters.restype = None
+    lib.orc_band_shape.argtypes = [P(abi.Config), C.c_uint64, P(C.c_uint64), P(C.c_uint64)]
+    lib.orc_band_shape.restype = None
+    lib.orc_barrier_from_bed.argtypes = [P(abi.Chrom), C.c_uint64, C.c_uint64, C.c_char, C.c_double,
+                                         C.c_double, C.c_double, P(abi.Barrier)]
+    lib.orc_barrier_from_bed.restype = C.c_int
+    lib.orc_xxh3_64.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, P(C.c_int)]
+    lib.orc_xxh3_64.restype = C.c_uint64
+    lib.orc_cell_seed.argtypes = [C.c_char_p, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64]
+    lib.orc_cell_seed.restype = C.c_uint64
+    lib.orc_libm_eval.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_uint64, C.c_double, C.c_double,
+                                  C.c_double, C.c_void_p, C.c_uint64]
+    lib.orc_libm_eval.restype = C.c_int
+    lib.orc_sample_streams.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_int, C.c_uint64, C.c_uint64,
+                                       C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_uint64]
+    lib.orc_sample_streams.restype = C.c_int
     _oracle = lib
     return lib
+
+
+class OracleHelpers:
+    """The host-side helpers of the engine's API (config defaults and transform, per-cell
+    seeds, LEF counts, task targets, band shapes, BED barriers), answered by the oracle
+    library alone.  ``modlefork_gb300.genome`` takes it as ``api=`` so that the CPU arm of the
+    benchmark builds its workload without loading the product library."""
+
+    def __init__(self):
+        from modlefork_gb300.engine import Chromosome
+
+        self.lib = load_oracle()
+        self.Chromosome = Chromosome
+
+    def config_defaults(self, **overrides):
+        cfg = abi.Config()
+        self.lib.orc_config_defaults(C.byref(cfg))
+        for k, v in overrides.items():
+            if not hasattr(cfg, k):
+                raise KeyError(k)
+            setattr(cfg, k, v)
+        return cfg
+
+    def config_transform(self, cfg):
+        rc = self.lib.orc_config_transform(C.byref(cfg))
+        if rc != 0:
+            raise ValueError(f"orc_config_transform returned {rc}")
+        return cfg
+
+    def cell_seed(self, name, chrom_size, seed, cell_id):
+        b = name.encode() if isinstance(name, str) else bytes(name)
+        return self.lib.orc_cell_seed(b, len(b), chrom_size, seed, cell_id)
+
+    def num_lefs(self, cfg, size_bp):
+        return self.lib.orc_num_lefs(C.byref(cfg), size_bp)
+
+    def band_shape(self, cfg, size_bp):
+        nr, nc = C.c_uint64(), C.c_uint64()
+        self.lib.orc_band_shape(C.byref(cfg), size_bp, C.byref(nr), C.byref(nc))
+        return nr.value, nc.value
+
+    def task_targets(self, cfg, size_bp, nlefs, ncells):
+        t = np.zeros(ncells, dtype=np.uint64)
+        e = C.c_uint64()
+        rc = self.lib.orc_task_targets(C.byref(cfg), size_bp, nlefs, ncells,
+                                       t.ctypes.data_as(C.POINTER(C.c_uint64)), C.byref(e))
+        if rc != 0:
+            raise ValueError(f"orc_task_targets returned {rc}")
+        return t, e.value
+
+    def barriers_from_bed(self, chrom, records, default_stp_active, default_stp_inactive):
+        ch = chrom.as_abi()
+        out = []
+        b = abi.Barrier()
+        for (s, e, strand, score) in records:
+            rc = self.lib.orc_barrier_from_bed(C.byref(ch), s, e, strand.encode(), float(score),
+                                               default_stp_active, default_stp_inactive, C.byref(b))
+            if rc < 0:
+                raise ValueError(f"orc_barrier_from_bed returned {rc}")
+            if rc == 1:
+                out.append(dict(pos=b.pos, stp_active=b.stp_active, stp_inactive=b.stp_inactive,
+                                blocking_dir=b.blocking_dir))
+        return out
+
+
+def tie_counters(enable=False, reset=False):
+    """Full-tie counters of the oracle's epoch-loop rank_lefs calls: (rank calls, calls with a
+    full tie, full-tie pairs, pairs away from the chromosome ends).  Counting stays on after a
+    call with ``enable`` true and is off otherwise."""
+    lib = load_oracle()
+    out = (C.c_uint64 * 4)()
+    lib.orc_tie_counters(1 if enable else 0, 1 if reset else 0, out)
+    return tuple(out)
 
 
 def oracle_pixels(band, nrows, ncols, bin_offset=0):
@@ -215,3 +305,40 @@ def check_golden(case, st):
     for key, want in exp.items():
         got = [int(x) for x in out[key]]
         assert got == [int(x) for x in want], f"{case['name']} {key}: got {got} want {want}"
+
+
+def host_libm(kind, x, y=None, mu=0.0, sigma=0.0, xi=0.0, threads=None):
+    """glibc's log / exp / pow / GEV noise / x < exp(y) through the oracle (the host side of
+    the device's mgpu_probe_libm)."""
+    lib = load_oracle()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    yp = None
+    if y is not None:
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        yp = y.ctypes.data
+    out = np.empty_like(x)
+    rc = lib.orc_libm_eval(kind, x.ctypes.data, yp, len(x), mu, sigma, xi, out.ctypes.data,
+                           threads or os.cpu_count() or 1)
+    assert rc == 0
+    return out
+
+
+# orc_sample kinds for the device probe kinds (engine.PROBE_*)
+ORACLE_SAMPLE_KIND = {0: 4, 1: 8, 2: 5, 3: 6, 4: 6, 5: 7}
+
+
+def host_samplers(probe_kind, seeds, per_stream, a0=0.0, a1=0.0, threads=None):
+    """The oracle's samplers (glibc) on the same seeded streams as engine.probe_samplers."""
+    lib = load_oracle()
+    seeds = np.ascontiguousarray(seeds, dtype=np.uint64)
+    out = np.empty((len(seeds), per_stream), dtype=np.float64)
+    draws = np.empty(len(seeds), dtype=np.uint64)
+    kind = ORACLE_SAMPLE_KIND[probe_kind]
+    if kind == 6:  # binomial(t = a, p)
+        a, b, p, q = int(a0), 0, a1, 0.0
+    else:  # normal(p, q), poisson(p), gev(0, p, q), exponential
+        a, b, p, q = 0, 0, a0, a1
+    rc = lib.orc_sample_streams(seeds.ctypes.data, len(seeds), per_stream, kind, a, b, p, q, out.ctypes.data,
+                                draws.ctypes.data, threads or os.cpu_count() or 1)
+    assert rc == 0
+    return out, draws

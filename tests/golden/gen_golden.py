@@ -259,9 +259,14 @@ def gen_xxh3(header):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    header = sys.argv[2] if len(sys.argv) > 2 else (
-        "/usr/local/lib/python3.12/dist-packages/pyarrow/include/arrow/vendored/xxhash/xxhash.h")
+    import argparse
+
+    ap = argparse.ArgumentParser(description="Re-extract the reference's known-answer cases and the "
+                                             "XXH3 vectors into tests/golden/.")
+    ap.add_argument("reference", help="root of the reference source tree (MoDLE)")
+    ap.add_argument("xxhash_header", help="path of an xxhash.h (xxHash 0.8.x) to build the vector generator")
+    args = ap.parse_args()
+    ref, header = args.reference, args.xxhash_header
     common = open(os.path.join(ref, "test/units/simulation_cpu/common.hpp")).read()
     default_seed = int(re.search(r"DEFAULT_PRNG\{random::PRNG\((\d+)ULL\)\}", common).group(1))
     cases = []

@@ -56,3 +56,20 @@ def test_committed_traffic_figures(kernel):
     assert d["bytes_per_lef_epoch"] == pytest.approx((d["dram_bytes_read"] + d["dram_bytes_write"]) / d["lef_epochs"],
                                                      rel=1e-3)
     assert traffic == pytest.approx(d["bytes_per_lef_epoch"] * 1_000_000.0)
+
+
+def test_reference_arm_loads_only_the_oracle():
+    """The CPU arm derives its workload (seeds, targets, barriers) through the oracle's helpers:
+    the product library stays unloaded in its process."""
+    code = (
+        "import sys, bench\n"
+        "from types import SimpleNamespace\n"
+        "bench.run_reference(SimpleNamespace(cells=4, steps=1, warmup=0, cpu_seconds=0.5, gpus=1))\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "from modlefork_gb300 import engine\n"
+        "print('PRODUCT' if ('libmgpu_modle' in maps or engine._lib is not None) else 'CLEAN')\n"
+        "print('ORACLE' if 'liboracle' in maps else 'NO-ORACLE')\n")
+    p = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert p.returncode == 0, p.stderr[-2000:]
+    out = p.stdout.strip().splitlines()
+    assert out[-2:] == ["CLEAN", "ORACLE"], out

@@ -168,3 +168,105 @@ def test_normal_tail_and_wedge_paths_are_exercised():
     draws = lib.orc_sample(C.c_uint64(99), 4, 0, 0, 0.0, 1.0, n, out.ctypes.data_as(C.POINTER(C.c_double)))
     assert np.abs(out).max() > 3.44  # beyond the tail start x_1
     assert 1.01 < draws / n < 1.06
+
+
+# ---- the oracle's own host helpers (used by the CPU arm instead of the product library) ----
+
+def test_oracle_cell_seed_matches_xxhash_vectors():
+    import json
+    import os
+
+    from _harness import GOLDEN, OracleHelpers
+
+    h = OracleHelpers()
+    vecs = json.load(open(os.path.join(GOLDEN, "xxh3_vectors.json")))["vectors"]
+    assert len(vecs) >= 1000
+    for v in vecs:
+        assert h.cell_seed(v["name"], v["size"], v["seed"], v["cell"]) == v["hash"], v
+
+
+def test_oracle_xxh3_every_short_length_matches_the_engine():
+    """Every input length the restatement covers (0..240 bytes) against the engine's own hash,
+    itself pinned by the xxHash vectors above; longer inputs are refused."""
+    from modlefork_gb300 import engine
+
+    lib = load_oracle()
+    elib = engine.load()
+    rng = np.random.default_rng(5)
+    ok = C.c_int()
+    for n in range(0, 241):
+        buf = rng.integers(0, 256, size=max(n, 1), dtype=np.uint8)
+        seed = int(rng.integers(0, 2**63))
+        got = lib.orc_xxh3_64(buf.ctypes.data, n, seed, C.byref(ok))
+        assert ok.value == 1
+        assert got == elib.mgpu_xxh3_64(buf.ctypes.data, n, seed), n
+    buf = np.zeros(241, dtype=np.uint8)
+    lib.orc_xxh3_64(buf.ctypes.data, 241, 0, C.byref(ok))
+    assert ok.value == 0
+
+
+def test_oracle_helpers_build_the_genome_workload_like_the_engine():
+    from _harness import OracleHelpers
+    from modlefork_gb300 import engine, genome
+
+    h = OracleHelpers()
+    cfg_o, gen_o = genome.genome_24chr(seed=11, nchroms=4, api=h)
+    cfg_e, gen_e = genome.genome_24chr(seed=11, nchroms=4)
+    assert bytes(cfg_o) == bytes(cfg_e)
+    for (co, bo), (ce, be) in zip(gen_o, gen_e):
+        assert bo == be
+        size = co.simulated_size
+        assert h.band_shape(cfg_o, size) == engine.band_shape(cfg_e, size)
+        nl = h.num_lefs(cfg_o, size)
+        assert nl == engine.num_lefs(cfg_e, size)
+        to, eo = h.task_targets(cfg_o, size, nl, 7)
+        te, ee = engine.task_targets(cfg_e, size, nl, 7)
+        assert list(to) == list(te) and eo == ee
+        for cell in (0, 1, 511):
+            assert h.cell_seed(co.name, co.size, cfg_o.seed, cell) == engine.cell_seed(ce.name, ce.size,
+                                                                                       cfg_e.seed, cell)
+    ch = engine.Chromosome("chr1", 1000, 100, 900)
+    recs = [(0, 50, "+", 0.0), (200, 201, "+", 0.0), (300, 303, "-", 0.9), (898, 900, "+", 0.0),
+            (899, 900, "-", 0.0)]
+    assert h.barriers_from_bed(ch, recs, 0.7, 0.7) == engine.barriers_from_bed(ch, recs, 0.7, 0.7)
+
+
+def test_full_tie_counter_counts_rank_calls_and_ties():
+    """Full ties (same position and binding epoch) are what the reference's tests leave unpinned
+    in the ranking; the oracle counts them per epoch-loop rank call.  On the parity workload
+    they appear in about 1 % of epochs, almost all of them units parked at a chromosome end."""
+    from _harness import OracleHelpers, tie_counters
+    from modlefork_gb300 import genome
+
+    h = OracleHelpers()
+    lib = load_oracle()
+    cfg, gen = genome.parity_10mbp(seed=7, api=h)
+    chrom, bars = gen[0]
+    nl = h.num_lefs(cfg, chrom.simulated_size)
+    targets, te = h.task_targets(cfg, chrom.simulated_size, nl, 64)
+    nr, nc = h.band_shape(cfg, chrom.simulated_size)
+    ch = make_chrom(chrom.start, chrom.end, chrom.size, chrom.name.encode())
+    bs = abi.make_barriers(bars)
+
+    def run(cells):
+        seeds = np.array([h.cell_seed(chrom.name, chrom.size, cfg.seed, i) for i in range(cells)],
+                         dtype=np.uint64)
+        band = np.zeros(nr * nc, dtype=np.uint32)
+        st = (abi.CellStats * cells)()
+        missed = C.c_uint64()
+        rc = lib.orc_simulate_cells_mt(C.byref(cfg), C.byref(ch), bs, len(bars),
+                                       seeds.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                       targets.ctypes.data_as(C.POINTER(C.c_uint64)), te, nl, cells, 4,
+                                       band.ctypes.data_as(C.POINTER(C.c_uint32)), C.byref(missed), st)
+        assert rc == 0
+        return sum(s.epochs for s in st)
+
+    tie_counters(enable=False, reset=True)
+    run(2)
+    assert tie_counters() == (0, 0, 0, 0)  # off: nothing counted
+    tie_counters(enable=True, reset=True)
+    epochs = run(16)
+    calls, tied, pairs, interior = tie_counters()
+    assert calls >= epochs  # one rank call per epoch (plus the first binding)
+    assert 0 < tied <= pairs and interior <= pairs
+    assert tied < 0.05 * calls
