@@ -94,10 +94,12 @@ int msur_assemble_input(const float* track, const float* params, int B, int L, i
  * reference's ContactMatrixDense layout): out[j][d] = log1p(band[j][d] * nrows / sum_d band[j][d])
  * per bin j (0 for a bin without contacts), computed in FP64 and stored as FP32. */
 int msur_band_target(const uint32_t* band, uint64_t ncols, int nrows, float* out, void* stream);
-/* Per-map sums for Pearson r and relative L2 (FP64, ADDED to out[6 * m .. 6 * m + 5]):
- * sum p, sum r, sum p^2, sum r^2, sum p r, sum (p - r)^2 over n values of map m. */
+/* Per-map sums for Pearson r and relative L2 (FP64, ADDED to out[6 * m .. 6 * m + 5]) over the n
+ * values of map m: sum p', sum r', sum p'^2, sum r'^2, sum p' r', sum (p - r)^2, where p' = p and
+ * r' = r when means is NULL and p' = p - means[2m], r' = r - means[2m + 1] otherwise (the second
+ * pass of the reference's two-pass Pearson, src/stats/correlation_impl.hpp:66-87). */
 int msur_map_sums(const float* pred, uint64_t pstride_map, const float* ref, uint64_t rstride_map, uint64_t n,
-                  int nmaps, double* out, void* stream);
+                  int nmaps, const double* means, double* out, void* stream);
 /* out[r][c] = in[r * stride + c] for c < n_valid (drop the padded channels of the head). */
 int msur_compact_rows(const float* in, int stride, uint64_t rows, int n_valid, float* out, void* stream);
 

@@ -534,21 +534,24 @@ __global__ void band_target_kernel(const uint32_t* band, size_t ncols, int nrows
 }
 
 // Per map m (n values each): sums for Pearson r and relative L2 of pred against ref, in FP64:
-// out[m] = {sum p, sum r, sum p^2, sum r^2, sum p r, sum (p - r)^2}.
+// out[m] = {sum p', sum r', sum p'^2, sum r'^2, sum p' r', sum (p - r)^2} with p' = p - mean_p,
+// r' = r - mean_r when means (2 per map) are given, the raw values otherwise: the two passes of
+// the reference's Pearson (mean, then covariances of the deviations).
 __global__ void map_sums_kernel(const float* pred, size_t pstride_map, const float* ref, size_t rstride_map,
-                                size_t n, double* out) {
+                                size_t n, const double* means, double* out) {
   const int m = blockIdx.y;
   const float* p = pred + m * pstride_map;
   const float* r = ref + m * rstride_map;
+  const double mp = means ? means[2 * m] : 0.0, mr = means ? means[2 * m + 1] : 0.0;
   double s[6] = {0, 0, 0, 0, 0, 0};
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const double a = p[i], b = r[i];
+    const double a = p[i] - mp, b = r[i] - mr;
     s[0] += a;
     s[1] += b;
     s[2] += a * a;
     s[3] += b * b;
     s[4] += a * b;
-    s[5] += (a - b) * (a - b);
+    s[5] += (static_cast<double>(p[i]) - r[i]) * (static_cast<double>(p[i]) - r[i]);
   }
   __shared__ double red[6][32];
   for (int k = 0; k < 6; ++k) {
@@ -866,10 +869,11 @@ int msur_band_target(const uint32_t* band, uint64_t ncols, int nrows, float* out
 }
 
 int msur_map_sums(const float* pred, uint64_t pstride_map, const float* ref, uint64_t rstride_map, uint64_t n,
-                  int nmaps, double* out, void* stream) {
+                  int nmaps, const double* means, double* out, void* stream) {
   if (!pred || !ref || !out || nmaps <= 0 || nmaps > 65535) return fail(MSUR_ERR_INVALID_ARG, "msur_map_sums: bad argument");
   dim3 grid(static_cast<unsigned>(std::min<uint64_t>((n + 255) / 256, 64)), nmaps);
-  map_sums_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(pred, pstride_map, ref, rstride_map, n, out);
+  map_sums_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(pred, pstride_map, ref, rstride_map, n,
+                                                                        means, out);
   return cuda_ok(cudaGetLastError(), "map_sums_kernel launch");
 }
 

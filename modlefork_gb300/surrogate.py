@@ -1,0 +1,358 @@
+"""The learned surrogate: a 1D U-Net neural operator from a window's barrier track and extrusion
+parameters to the expected banded contact map the simulator converges to.
+
+Every arithmetic step runs in the library's own kernels (libmgpu_surrogate.so): the
+convolutions on the tensor cores (tcgen05, BF16 operands, FP32 accumulators), pooling,
+upsampling, losses, gradients and Adam in hand-written CUDA.  torch only provides device memory
+and the stream; there is no autograd: the backward pass is written out layer by layer below.
+
+Architecture (``UNet(widths=(64, 128, 256, 384, 512), mid=512)``, about 8.9 M parameters):
+
+* input: [B, 4000, 64] BF16, channels 0-3 the barrier track (summed occupancy, + motifs,
+  - motifs, LEF density), 4-7 the parameter vector, the rest zero;
+* encoder level i (length 4000 / 2^i): two 3-tap convolutions with SiLU, then average pooling
+  by two; a bottleneck of two 3-tap convolutions at 125 positions;
+* decoder level i: nearest upsampling by two concatenated with the encoder's level-i output,
+  two 3-tap convolutions with SiLU;
+* head: a 1-tap convolution to 640 channels of which the first 600 are the band's diagonals
+  d = 0..599 of each bin, in FP32: the output is the band in its own column-major layout
+  (ContactMatrixDense, contact_matrix_dense_impl.hpp:40-51), as the row-normalised log1p target.
+
+Training minimises the mean squared error against simulated targets with Adam; evaluation
+scores every map by Pearson r and relative L2 against fresh simulator runs, and a map whose r
+falls below the gate (0.95) is answered by the simulator instead.
+"""
+
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import surrogate_ops as ops
+
+NROWS = 600     # diagonals of the band (3 Mbp at 5 kb)
+HEAD_PAD = 640  # head channels: the 600 diagonals padded to the tile width
+IN_CH = 64      # input channels (8 used, padded to the tensor cores' K step)
+LOSS_SCALE = 1024.0
+
+
+def _align(n, a=64):
+    return (n + a - 1) // a * a
+
+
+class ConvSpec:
+    def __init__(self, name, cout, taps, cin, act=True):
+        self.name, self.cout, self.taps, self.cin, self.act = name, cout, taps, cin, act
+
+    @property
+    def wsize(self):
+        return self.cout * self.taps * self.cin
+
+
+def conv_specs(widths, mid):
+    """The network's convolutions in order: two per encoder level, two in the bottleneck, two
+    per decoder level (deepest first), then the head."""
+    specs = []
+    cin = IN_CH
+    for i, w in enumerate(widths):
+        specs += [ConvSpec(f"enc{i}a", w, 3, cin), ConvSpec(f"enc{i}b", w, 3, w)]
+        cin = w
+    specs += [ConvSpec("mid_a", mid, 3, cin), ConvSpec("mid_b", mid, 3, mid)]
+    ch = mid
+    for i in reversed(range(len(widths))):
+        w = widths[i]
+        specs += [ConvSpec(f"dec{i}a", w, 3, ch + w), ConvSpec(f"dec{i}b", w, 3, w)]
+        ch = w
+    specs.append(ConvSpec("head", HEAD_PAD, 1, widths[0], act=False))
+    return specs
+
+
+class UNet:
+    """Parameters, optimiser state and per-batch-size workspaces of the surrogate network."""
+
+    def __init__(self, widths=(64, 128, 256, 384, 512), mid=512, length=4000, device=0, seed=0, head_bias=None):
+        self.widths = tuple(widths)
+        self.mid = mid
+        self.depth = len(widths)
+        if length % (1 << self.depth):
+            raise ValueError(f"length {length} must be divisible by 2^{self.depth}")
+        self.length = length
+        self.dev = torch.device("cuda", device)
+        specs = conv_specs(self.widths, mid)
+        self.specs = {s.name: s for s in specs}
+        # one flat FP32 buffer of parameters (each weight and bias 64-element aligned, so every
+        # BF16 view starts 16-byte aligned for TMA), its gradient, Adam moments and BF16 copy
+        offs, n = {}, 0
+        for s in specs:
+            offs[s.name] = (n, n + _align(s.wsize))
+            n = offs[s.name][1] + _align(s.cout)
+        self.nparams_padded = n
+        self.nparams = sum(s.wsize + s.cout for s in specs)
+        kw = dict(device=self.dev)
+        self.p = torch.zeros(n, dtype=torch.float32, **kw)
+        self.g = torch.zeros(n, dtype=torch.float32, **kw)
+        self.m = torch.zeros(n, dtype=torch.float32, **kw)
+        self.v = torch.zeros(n, dtype=torch.float32, **kw)
+        self.pb = torch.zeros(n, dtype=torch.bfloat16, **kw)
+        self.w32, self.b32, self.wb, self.gw, self.gb, self.wt = {}, {}, {}, {}, {}, {}
+        for s in specs:
+            wo, bo = offs[s.name]
+            shape = (s.cout, s.taps, s.cin)
+            self.w32[s.name] = self.p[wo:wo + s.wsize].view(shape)
+            self.b32[s.name] = self.p[bo:bo + s.cout]
+            self.wb[s.name] = self.pb[wo:wo + s.wsize].view(shape)
+            self.gw[s.name] = self.g[wo:wo + s.wsize].view(shape)
+            self.gb[s.name] = self.g[bo:bo + s.cout]
+            self.wt[s.name] = torch.empty(s.cin, s.taps, s.cout, dtype=torch.bfloat16, **kw)
+        self.step_count = 0
+        self._ws = {}
+        self._init(seed, head_bias)
+
+    # ---- parameters ----------------------------------------------------------------------
+    def _init(self, seed, head_bias):
+        rng = np.random.default_rng(seed)
+        host = np.zeros(self.nparams_padded, dtype=np.float32)
+        for name, s in self.specs.items():
+            wo = self.w32[name].data_ptr() - self.p.data_ptr()
+            wo //= 4
+            fan_in = s.taps * s.cin
+            gain = 1.6 if s.act else 0.02  # SiLU keeps about 0.36 of the variance; a quiet head
+            host[wo:wo + s.wsize] = rng.standard_normal(s.wsize) * gain / math.sqrt(fan_in)
+        self.p.copy_(torch.from_numpy(host))
+        if head_bias is not None:
+            hb = torch.zeros(HEAD_PAD, dtype=torch.float32)
+            hb[:NROWS] = torch.as_tensor(np.asarray(head_bias, dtype=np.float32))
+            self.b32["head"].copy_(hb)
+        self.pb.copy_(self.p)
+        self._refresh_transposes()
+
+    def _refresh_transposes(self):
+        for name in self.specs:
+            ops.weight_transpose(self.wb[name], self.wt[name])
+
+    def params_dict(self):
+        """name -> (w [Cout, taps, Cin], b [Cout]) as numpy float32 copies."""
+        return {k: (self.w32[k].cpu().numpy(), self.b32[k].cpu().numpy()) for k in self.specs}
+
+    def state_dict(self):
+        return {"widths": np.array(self.widths), "mid": np.array(self.mid), "length": np.array(self.length),
+                "params": self.p.cpu().numpy()}
+
+    def load_state(self, state):
+        p = torch.as_tensor(np.asarray(state["params"], dtype=np.float32))
+        if p.numel() != self.p.numel():
+            raise ValueError("parameter count differs from this network's")
+        self.p.copy_(p)
+        self.pb.copy_(self.p)
+        self._refresh_transposes()
+
+    @classmethod
+    def from_state(cls, state, device=0):
+        net = cls(widths=tuple(int(w) for w in state["widths"]), mid=int(state["mid"]), length=int(state["length"]),
+                  device=device)
+        net.load_state(state)
+        return net
+
+    # ---- workspaces ----------------------------------------------------------------------
+    def _workspace(self, B, train):
+        key = (B, train)
+        if key in self._ws:
+            return self._ws[key]
+        kw = dict(dtype=torch.bfloat16, device=self.dev)
+        L, D = self.length, self.depth
+        ws = {"x": torch.empty(B, L, IN_CH, **kw), "out": torch.empty(B, L, NROWS, dtype=torch.float32, device=self.dev)}
+        lens = [L >> i for i in range(D + 1)]
+        for i, w in enumerate(self.widths):
+            for k in ("za", "ya", "zb", "yb"):
+                if train or k in ("ya", "yb"):
+                    ws[f"{k}{i}"] = torch.empty(B, lens[i], w, **kw)
+            ws[f"p{i}"] = torch.empty(B, lens[i + 1], w, **kw)
+            ch = self.mid if i == D - 1 else self.widths[i + 1]
+            ws[f"cat{i}"] = torch.empty(B, lens[i], ch + w, **kw)
+            for k in ("zda", "yda", "zdb", "ydb"):
+                if train or k in ("yda", "ydb"):
+                    ws[f"{k}{i}"] = torch.empty(B, lens[i], w, **kw)
+        for k in ("zma", "yma", "zmb", "ymb"):
+            if train or k in ("yma", "ymb"):
+                ws[k] = torch.empty(B, lens[D], self.mid, **kw)
+        if train:
+            ws["dout"] = torch.empty(B, L, HEAD_PAD, **kw)
+            ws["loss"] = torch.zeros(1, dtype=torch.float64, device=self.dev)
+            for i, w in enumerate(self.widths):
+                ch = self.mid if i == D - 1 else self.widths[i + 1]
+                ws[f"dcat{i}"] = torch.empty(B, lens[i], ch + w, **kw)
+                ws[f"dzb{i}"] = torch.empty(B, lens[i], w, **kw)   # encoder b, and the decoder's
+                ws[f"dza{i}"] = torch.empty(B, lens[i], w, **kw)   # gradients reuse them per level
+                ws[f"ddb{i}"] = torch.empty(B, lens[i], w, **kw)
+                ws[f"dda{i}"] = torch.empty(B, lens[i], w, **kw)
+                ws[f"dp{i}"] = torch.empty(B, lens[i + 1], w, **kw)
+            ws["dmb"] = torch.empty(B, lens[D], self.mid, **kw)
+            ws["dma"] = torch.empty(B, lens[D], self.mid, **kw)
+        self._ws[key] = ws
+        return ws
+
+    # ---- forward -------------------------------------------------------------------------
+    def _conv(self, name, x, pre=None, post=None, f32=None, **kw):
+        s = self.specs[name]
+        ops.conv_forward(x, self.wb[name], bias=self.b32[name], act=ops.ACT_SILU if s.act else ops.ACT_NONE,
+                         out_pre=pre, out_post=post, out_f32=f32, **kw)
+
+    def forward(self, x, train=False):
+        """x: [B, L, 64] BF16 input; returns the [B, L, 600] FP32 prediction (a workspace view)."""
+        B = x.shape[0]
+        ws = self._workspace(B, train)
+        get = (lambda k: ws.get(k)) if train else (lambda k: None)
+        h = x
+        ws["h_in0"] = x
+        for i in range(self.depth):
+            self._conv(f"enc{i}a", h, pre=get(f"za{i}"), post=ws[f"ya{i}"])
+            self._conv(f"enc{i}b", ws[f"ya{i}"], pre=get(f"zb{i}"), post=ws[f"yb{i}"])
+            ops.pool2(ws[f"yb{i}"], ws[f"p{i}"])
+            h = ws[f"p{i}"]
+        self._conv("mid_a", h, pre=get("zma"), post=ws["yma"])
+        self._conv("mid_b", ws["yma"], pre=get("zmb"), post=ws["ymb"])
+        h = ws["ymb"]
+        for i in reversed(range(self.depth)):
+            ops.upcat(h, ws[f"yb{i}"], ws[f"cat{i}"])
+            self._conv(f"dec{i}a", ws[f"cat{i}"], pre=get(f"zda{i}"), post=ws[f"yda{i}"])
+            self._conv(f"dec{i}b", ws[f"yda{i}"], pre=get(f"zdb{i}"), post=ws[f"ydb{i}"])
+            h = ws[f"ydb{i}"]
+        self._conv("head", h, f32=ws["out"], n_valid=NROWS, out_stride=NROWS)
+        return ws["out"]
+
+    # ---- backward ------------------------------------------------------------------------
+    def _grads(self, name, x, dz):
+        """Weight and bias gradients of convolution `name` with input x and output gradient dz."""
+        ops.conv_wgrad(x, dz, self.gw[name])
+        ops.bias_grad(dz, self.gb[name])
+
+    def _dgrad(self, name, dz, out, gate=None):
+        ops.conv_forward(dz, self.wt[name], out_post=out, gate=gate)
+
+    def backward(self, B):
+        """Gradients of the last training forward pass into self.g (after ws['dout'] is set)."""
+        ws = self._ws[(B, True)]
+        D = self.depth
+        self._grads("head", ws["ydb0"], ws["dout"])
+        self._dgrad("head", ws["dout"], ws["ddb0"], gate=ws["zdb0"])
+        for i in range(D):
+            self._grads(f"dec{i}b", ws[f"yda{i}"], ws[f"ddb{i}"])
+            self._dgrad(f"dec{i}b", ws[f"ddb{i}"], ws[f"dda{i}"], gate=ws[f"zda{i}"])
+            self._grads(f"dec{i}a", ws[f"cat{i}"], ws[f"dda{i}"])
+            self._dgrad(f"dec{i}a", ws[f"dda{i}"], ws[f"dcat{i}"])
+            if i + 1 < D:
+                ops.upcat_bwd(ws[f"dcat{i}"], ws[f"zdb{i + 1}"], ws[f"ddb{i + 1}"])
+            else:
+                ops.upcat_bwd(ws[f"dcat{i}"], ws["zmb"], ws["dmb"])
+        self._grads("mid_b", ws["yma"], ws["dmb"])
+        self._dgrad("mid_b", ws["dmb"], ws["dma"], gate=ws["zma"])
+        self._grads("mid_a", ws[f"p{D - 1}"], ws["dma"])
+        self._dgrad("mid_a", ws["dma"], ws[f"dp{D - 1}"])
+        for i in reversed(range(D)):
+            ch = self.mid if i == D - 1 else self.widths[i + 1]
+            ops.skip_grad(ws[f"zb{i}"], ws[f"dzb{i}"], dpool=ws[f"dp{i}"], dcat=ws[f"dcat{i}"], cat_off=ch)
+            self._grads(f"enc{i}b", ws[f"ya{i}"], ws[f"dzb{i}"])
+            self._dgrad(f"enc{i}b", ws[f"dzb{i}"], ws[f"dza{i}"], gate=ws[f"za{i}"])
+            x_in = ws["h_in0"] if i == 0 else ws[f"p{i - 1}"]
+            self._grads(f"enc{i}a", x_in, ws[f"dza{i}"])
+            if i > 0:
+                self._dgrad(f"enc{i}a", ws[f"dza{i}"], ws[f"dp{i - 1}"])
+
+    def loss_and_grad(self, x, target):
+        """Forward, MSE loss against target [B, L, 600] and gradients in self.g (scaled by
+        LOSS_SCALE); returns the loss as a device scalar (FP64 sum of squares / count)."""
+        B = x.shape[0]
+        ws = self._workspace(B, True)
+        out = self.forward(x, train=True)
+        n = B * self.length * NROWS
+        ws["loss"].zero_()
+        self.g.zero_()
+        ops.mse(out, target, ws["loss"], dp=ws["dout"], scale=2.0 * LOSS_SCALE / n)
+        self.backward(B)
+        return ws["loss"] / n
+
+    def adam_step(self, lr, b1=0.9, b2=0.999, eps=1e-8, wd=0.0):
+        self.step_count += 1
+        ops.adam(self.p, self.g, self.m, self.v, self.step_count, lr, b1, b2, eps, wd, gscale=1.0 / LOSS_SCALE,
+                 p_bf16=self.pb)
+        self._refresh_transposes()
+
+    def flops_per_map(self, backward=False):
+        """Multiply-adds x 2 of one map's forward pass (x 3 with the backward pass)."""
+        f = 0
+        for name, s in self.specs.items():
+            level = 0
+            if name.startswith(("enc", "dec")):
+                level = int(name[3])
+            elif name.startswith("mid"):
+                level = self.depth
+            f += 2 * (self.length >> level) * s.cout * s.taps * s.cin
+        return f * (3 if backward else 1)
+
+
+# ---------------------------------------------------------------------------------------------
+class Dataset:
+    """Inputs and targets resident on the device: x [N, L, 64] BF16, target [N, L, 600] FP32."""
+
+    def __init__(self, track, params, target, device=0):
+        dev = torch.device("cuda", device)
+        self.track = torch.as_tensor(track).to(dev, torch.float32).contiguous()
+        self.params = torch.as_tensor(params).to(dev, torch.float32).contiguous()
+        self.target = torch.as_tensor(target).to(dev, torch.float32).contiguous()
+        N, _, L = self.track.shape
+        self.x = torch.empty(N, L, IN_CH, dtype=torch.bfloat16, device=dev)
+        ops.assemble_input(self.track, self.params, self.x)
+
+    def __len__(self):
+        return self.x.shape[0]
+
+    def diagonal_mean(self):
+        """Mean target per diagonal over all maps and bins: the distance-decay baseline."""
+        return self.target.double().mean(dim=(0, 1)).float().cpu().numpy()
+
+
+def train(net, data, steps, batch=16, lr=2e-3, lr_min=2e-5, warmup=100, seed=0, log=None, log_every=200):
+    """Adam on the MSE with a linear warm-up and cosine decay; returns per-step losses."""
+    rng = np.random.default_rng(seed)
+    N = len(data)
+    xb = torch.empty(batch, net.length, IN_CH, dtype=torch.bfloat16, device=net.dev)
+    tb = torch.empty(batch, net.length, NROWS, dtype=torch.float32, device=net.dev)
+    losses = []
+    t0 = time.perf_counter()
+    for step in range(steps):
+        idx = torch.from_numpy(rng.choice(N, size=batch, replace=N < batch)).to(net.dev)
+        torch.index_select(data.x, 0, idx, out=xb)
+        torch.index_select(data.target, 0, idx, out=tb)
+        loss = net.loss_and_grad(xb, tb)
+        if step < warmup:
+            cur = lr * (step + 1) / warmup
+        else:
+            cur = lr_min + 0.5 * (lr - lr_min) * (1 + math.cos(math.pi * (step - warmup) / max(1, steps - warmup)))
+        net.adam_step(cur)
+        losses.append(loss)
+        if log and (step % log_every == 0 or step == steps - 1):
+            log(f"step {step}: loss {loss.item():.5f} lr {cur:.2e} ({time.perf_counter() - t0:.1f} s)")
+    return torch.stack(losses).cpu().numpy().ravel()
+
+
+def predict(net, x, batch=256):
+    """Predictions [N, L, 600] FP32 for inputs x [N, L, 64] in batches."""
+    out = torch.empty(x.shape[0], net.length, NROWS, dtype=torch.float32, device=net.dev)
+    for i in range(0, x.shape[0], batch):
+        j = min(x.shape[0], i + batch)
+        out[i:j].copy_(net.forward(x[i:j], train=False))
+    return out
+
+
+def evaluate(pred, target):
+    """Per-map Pearson r and relative L2 error of predictions against targets (both [N, L, 600])."""
+    n = pred.shape[1] * pred.shape[2]
+    return ops.map_scores(pred, target, n, pred.shape[0])
+
+
+def baseline_prediction(diag_mean, n, length, device):
+    """The method without the network: every bin predicted by the training set's mean target
+    per diagonal (the distance-decay curve)."""
+    row = torch.as_tensor(np.asarray(diag_mean, dtype=np.float32), device=device)
+    return row.view(1, 1, NROWS).expand(n, length, NROWS).contiguous()

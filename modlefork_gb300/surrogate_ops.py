@@ -9,6 +9,7 @@ BF16 [Cout, taps, Cin].
 import ctypes as C
 import os
 
+import numpy as np
 import torch
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libmgpu_surrogate.so")
@@ -43,7 +44,7 @@ def load(path=LIB_PATH):
         "msur_weight_transpose": (i32, [vp, i32, i32, i32, vp, vp]),
         "msur_assemble_input": (i32, [vp, vp, i32, i32, i32, vp, vp]),
         "msur_band_target": (i32, [vp, u64, i32, vp, vp]),
-        "msur_map_sums": (i32, [vp, u64, vp, u64, u64, i32, vp, vp]),
+        "msur_map_sums": (i32, [vp, u64, vp, u64, u64, i32, vp, vp, vp]),
         "msur_compact_rows": (i32, [vp, i32, u64, i32, vp, vp]),
     }
     for name, (res, args) in sigs.items():
@@ -156,10 +157,28 @@ def band_target(band, ncols, nrows, out):
     _check(load().msur_band_target(_p(band), ncols, nrows, _p(out), _stream()), "msur_band_target")
 
 
-def map_sums(pred, ref, n, nmaps, out, pstride=None, rstride=None):
+def map_sums(pred, ref, n, nmaps, out, pstride=None, rstride=None, means=None):
     pstride = pstride if pstride is not None else n
     rstride = rstride if rstride is not None else n
-    _check(load().msur_map_sums(_p(pred), pstride, _p(ref), rstride, n, nmaps, _p(out), _stream()), "msur_map_sums")
+    _check(load().msur_map_sums(_p(pred), pstride, _p(ref), rstride, n, nmaps, _p(means), _p(out), _stream()),
+           "msur_map_sums")
+
+
+def map_scores(pred, ref, n, nmaps, pstride=None, rstride=None):
+    """Per-map Pearson r (two passes: means, then covariances of the deviations, clamped to
+    [-1, 1], as src/stats/correlation_impl.hpp:66-87 computes it) and relative L2 error
+    ||p - r|| / ||r||, both in FP64 on the device.  Returns two numpy arrays of nmaps values."""
+    dev = pred.device
+    s1 = torch.zeros(nmaps, 6, dtype=torch.float64, device=dev)
+    map_sums(pred, ref, n, nmaps, s1, pstride, rstride)
+    means = (s1[:, :2] / n).contiguous()
+    s2 = torch.zeros(nmaps, 6, dtype=torch.float64, device=dev)
+    map_sums(pred, ref, n, nmaps, s2, pstride, rstride, means=means)
+    s2 = s2.cpu().numpy()
+    raw = s1.cpu().numpy()
+    r = np.clip(s2[:, 4] / np.sqrt(s2[:, 2] * s2[:, 3]), -1.0, 1.0)
+    rel_l2 = np.sqrt(s2[:, 5] / raw[:, 3])
+    return r, rel_l2
 
 
 def compact_rows(inp, n_valid, out):

@@ -273,6 +273,10 @@ def test_band_target_and_map_scores():
     want = np.stack([A.sum(1), Bm.sum(1), (A * A).sum(1), (Bm * Bm).sum(1), (A * Bm).sum(1),
                      ((A - Bm) ** 2).sum(1)], 1)
     assert np.allclose(sn, want, rtol=1e-10, atol=1e-8)
+    r, rel = ops.map_scores(torch.from_numpy(a).to(DEV), torch.from_numpy(b).to(DEV), 1000, 3)
+    for m in range(3):
+        assert abs(r[m] - np.corrcoef(A[m], Bm[m])[0, 1]) < 1e-12
+        assert abs(rel[m] - np.linalg.norm(A[m] - Bm[m]) / np.linalg.norm(Bm[m])) < 1e-12
     # compacting the head's padded rows
     pad = torch.from_numpy(rng.standard_normal((2, 5, 640)).astype(np.float32)).to(DEV)
     dense = torch.empty(2, 5, 600, dtype=torch.float32, device=DEV)
