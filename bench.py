@@ -55,6 +55,10 @@ def parse_args():
     ap.add_argument("--smem-budget", type=int, default=None, help="shared memory per cell (bytes)")
     ap.add_argument("--carveout", type=int, default=None, help="shared-memory carveout percent")
     ap.add_argument("--batched", type=int, default=1, help="also time the one-launch batched engine")
+    ap.add_argument("--windows", type=int, default=64,
+                    help="windows of the batched uneven-window workload timed in one launch (0 = skip)")
+    ap.add_argument("--surrogate", type=int, default=1, help="also time the learned surrogate against the simulator")
+    ap.add_argument("--sur-maps", type=int, default=16, help="fresh simulator maps the surrogate is scored on")
     return ap.parse_args()
 
 
@@ -122,12 +126,141 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
-def measured_peak():
+def measured_peak(key="hbm_gbs"):
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
         d = json.load(open(path))
-        return float(d["hbm_gbs"]), "measured"
-    return 6800.0, "fallback"
+        return float(d[key]), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}[key], "fallback"
+
+
+SUR_HELD_BASE = 2_000_000  # parameter sets neither the training nor its evaluation used
+
+
+def run_windows(args, device, log):
+    """The batched workload of uneven windows: the first ``args.windows`` of the 4096 seeded
+    windows (lengths log-uniform in [1, 250] Mbp, bin 1-10 kb, LEF and barrier densities
+    U(5, 40)/Mbp, each with its own configuration) x 256 cells in one batched launch.  A sample
+    of cells is re-simulated by plain per-window launches on engines created with each window's
+    configuration and must give identical per-cell results."""
+    import torch
+
+    from modlefork_gb300 import engine, genome
+
+    cells = 256
+    wins = genome.batched_windows(seed=13, nwindows=args.windows, cells=cells)
+    dev = torch.device("cuda", device)
+    with engine.Engine(genome.genome_config(), device) as eng:
+        tasks, bands, meta = [], {}, []
+        for cfg, chrom, bars in wins:
+            cid = eng.upload_chrom(chrom, bars)
+            eng.set_chrom_config(cid, cfg)
+            nl = engine.num_lefs(cfg, chrom.simulated_size)
+            tg, te = engine.task_targets(cfg, chrom.simulated_size, nl, cells)
+            nrows, ncols = engine.band_shape(cfg, chrom.simulated_size)
+            bands[cid] = torch.zeros(nrows * ncols, dtype=torch.int32, device=dev)
+            seeds = [engine.cell_seed(chrom.name, chrom.size, cfg.seed, i) for i in range(cells)]
+            meta.append((cfg, chrom, bars, nl, seeds, [int(x) for x in tg], te, len(tasks)))
+            tasks += [(cid, sd, int(t), te, nl) for sd, t in zip(seeds, tg)]
+        dbands = {c: b.data_ptr() for c, b in bands.items()}
+        torch.cuda.synchronize()
+        log(f"uneven windows: {len(wins)} windows x {cells} cells in one batched launch")
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        _, st = eng.simulate_batch(tasks, dbands)
+        ev1.record()
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+    # sampled bit-exactness: the cheapest windows' first two cells through plain launches
+    order = sorted(range(len(meta)), key=lambda k: meta[k][3] * meta[k][6])[:4]
+    compared = equal = 0
+    for k in order:
+        cfg, chrom, bars, nl, seeds, tg, te, first = meta[k]
+        with engine.Engine(cfg, device) as eng:
+            cid = eng.upload_chrom(chrom, bars)
+            _, pst = eng.simulate_cells(cid, np.array(seeds[:2], dtype=np.uint64), np.array(tg[:2], dtype=np.uint64),
+                                        te, nl)
+        for i in range(2):
+            a, b = pst[i], st[first + i]
+            compared += 1
+            equal += int((a.epochs, a.burnin_epochs, a.contacts, a.missed_updates, a.lef_epochs, a.rng_draws) ==
+                         (b.epochs, b.burnin_epochs, b.contacts, b.missed_updates, b.lef_epochs, b.rng_draws))
+    le = sum(x.lef_epochs for x in st)
+    return {"windows": len(wins), "of_windows": 4096, "cells_per_window": cells, "cells": len(st),
+            "window_mbp": float(sum(w[1].size for w in wins) / 1e6),
+            "bin_sizes_kb": sorted({int(w[0].bin_size // 1000) for w in wins}),
+            "ms": ms, "value": le / (ms / 1e3), "unit": "LEF-epochs/s", "cells_per_s": len(st) / (ms / 1e3),
+            "contacts_per_s": sum(x.contacts for x in st) / (ms / 1e3), "launches": 1,
+            "parity_sample": {"cells": compared, "equal": equal,
+                              "against": "plain per-window launches on engines with each window's configuration"},
+            "note": "the first windows of the seeded 4096-window workload; the whole workload (about 2e12 "
+                    "LEF-epochs) takes about 40 minutes at this rate"}
+
+
+def run_surrogate(args, log):
+    """The learned surrogate against the batched simulator on fresh 20 Mbp windows: the
+    committed network (modlefork_gb300/data/surrogate_unet.npz) predicts each window's map,
+    scored by Pearson r and relative L2 against the simulator's map of the same window (1024
+    cells, contact density 10); maps below the r gate fall back to the simulator.  maps/s of the
+    surrogate at inference batch 256 (inputs resident, CUDA events) and end to end (host inputs
+    in, predicted maps back to host memory), against the simulator's maps/s on these windows."""
+    import torch
+
+    from modlefork_gb300 import surrogate as S
+    from modlefork_gb300 import sweep
+    from modlefork_gb300 import train_surrogate as T
+
+    net = T.load_weights(os.path.join(ROOT, "modlefork_gb300", "data", "surrogate_unet.npz"))
+    n = args.sur_maps
+    log(f"surrogate: simulating {n} fresh windows")
+    sims = sweep.simulate_sets(list(range(SUR_HELD_BASE, SUR_HELD_BASE + n)), cells=1024, density=10.0)
+    data = S.Dataset(sims["track"], sims["params"], sims["target"], net.dev)
+    r, rel = S.evaluate(S.predict(net, data.x), data.target)
+    sim_mps = n / (sims["ms"] / 1e3)
+    log("surrogate: inference")
+    mps, ms, tf = T.inference_rate(net, data.x, batch=256, reps=20)
+    # end to end: host track and parameters in, 256 predicted maps back to pinned host memory
+    B = 256
+    idx = np.arange(B) % n
+    h_track = sims["track"].cpu().numpy()[idx].copy()
+    h_params = sims["params"].cpu().numpy()[idx].copy()
+    pin_track = torch.from_numpy(h_track).pin_memory()
+    pin_params = torch.from_numpy(h_params).pin_memory()
+    pin_out = torch.empty(B, net.length, S.NROWS, dtype=torch.float32).pin_memory()
+    d_track = torch.empty(pin_track.shape, dtype=torch.float32, device=net.dev)
+    d_params = torch.empty(pin_params.shape, dtype=torch.float32, device=net.dev)
+    d_x = torch.empty(B, net.length, S.IN_CH, dtype=torch.bfloat16, device=net.dev)
+    reps = 5
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        d_track.copy_(pin_track, non_blocking=True)
+        d_params.copy_(pin_params, non_blocking=True)
+        S.ops.assemble_input(d_track, d_params, d_x)
+        pin_out.copy_(net.forward(d_x), non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_mps = B * reps / (time.perf_counter() - t0)
+    passed = r >= 0.95
+    tpeak, tkind = measured_peak("bf16_tflops")
+    eff = 1.0 / (1.0 / mps + (1.0 - passed.mean()) / sim_mps)
+    return {
+        "metric": "maps/s", "value": mps, "unit": "maps/s", "batch": B, "ms_per_batch": ms,
+        "maps_scored": n, "mean_r": float(r.mean()), "min_r": float(r.min()), "mean_rel_l2": float(rel.mean()),
+        "gate_r": 0.95, "maps_passing_gate": int(passed.sum()),
+        "gated_maps_per_s": eff, "simulator_maps_per_s": sim_mps, "over_simulator": mps / sim_mps,
+        "gated_over_simulator": eff / sim_mps,
+        "simulator_config": "20 Mbp windows of the sweep generator, 1024 cells, contact density 10, one batched "
+                            "launch (CUDA events around the launch)",
+        "fp64_target_check_max_rel_dev": sims["fp64_max_rel_dev"],
+        "e2e": {"value": e2e_mps, "unit": "maps/s",
+                "h2d_bytes_per_step": int(h_track.nbytes + h_params.nbytes),
+                "d2h_bytes_per_step": int(pin_out.numel() * 4)},
+        "roofline": {"bound": "tensor", "achieved": tf, "peak": tpeak, "unit": "TFLOP/s", "frac": tf / tpeak,
+                     "peak_source": f"{tkind} bf16_tflops", "flops_model": "2 x multiply-adds of the network's "
+                     f"convolutions per map ({net.flops_per_map() / 1e9:.2f} GFLOP) x maps / time",
+                     "traffic": None},
+        "nparams": net.nparams, "dtype": "bf16 operands, fp32 accumulate",
+    }
 
 
 def dram_traffic_per_launch(lef_epochs_per_launch, kernel="simulate_kernel"):
@@ -545,6 +678,10 @@ def run_ours(args):
     }
     if batched is not None:
         line["batched"]["over_plain_wave_cells_per_s"] = batched["cells_per_s"] / line["cells_per_s"]
+    if args.windows > 0:
+        line["batched_windows"] = run_windows(args, local, log)
+    if args.surrogate:
+        line["surrogate"] = run_surrogate(args, log)
     if not args.no_cpu_baseline:
         log("cpu baseline")
         threads = os.cpu_count() or 1

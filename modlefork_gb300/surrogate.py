@@ -296,7 +296,7 @@ class Dataset:
     """Inputs and targets resident on the device: x [N, L, 64] BF16, target [N, L, 600] FP32."""
 
     def __init__(self, track, params, target, device=0):
-        dev = torch.device("cuda", device)
+        dev = device if isinstance(device, torch.device) else torch.device("cuda", device)
         self.track = torch.as_tensor(track).to(dev, torch.float32).contiguous()
         self.params = torch.as_tensor(params).to(dev, torch.float32).contiguous()
         self.target = torch.as_tensor(target).to(dev, torch.float32).contiguous()
