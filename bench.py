@@ -55,7 +55,7 @@ def parse_args():
     ap.add_argument("--smem-budget", type=int, default=None, help="shared memory per cell (bytes)")
     ap.add_argument("--carveout", type=int, default=None, help="shared-memory carveout percent")
     ap.add_argument("--batched", type=int, default=1, help="also time the one-launch batched engine")
-    ap.add_argument("--windows", type=int, default=64,
+    ap.add_argument("--windows", type=int, default=16,
                     help="windows of the batched uneven-window workload timed in one launch (0 = skip)")
     ap.add_argument("--surrogate", type=int, default=1, help="also time the learned surrogate against the simulator")
     ap.add_argument("--sur-maps", type=int, default=16, help="fresh simulator maps the surrogate is scored on")
@@ -193,8 +193,10 @@ def run_windows(args, device, log):
             "contacts_per_s": sum(x.contacts for x in st) / (ms / 1e3), "launches": 1,
             "parity_sample": {"cells": compared, "equal": equal,
                               "against": "plain per-window launches on engines with each window's configuration"},
-            "note": "the first windows of the seeded 4096-window workload; the whole workload (about 2e12 "
-                    "LEF-epochs) takes about 40 minutes at this rate"}
+            "note": "the first windows of the seeded 4096-window workload (a stated subset); the whole "
+                    "workload is about 2e12 LEF-epochs.  One warp advances one cell, so the launch's tail "
+                    "is the longest cell: the fourth window (170 Mbp at 1 kb bins, 6450 LEFs, about 1e4 epochs per "
+                    "cell) sets this subset's time"}
 
 
 def run_surrogate(args, log):
@@ -634,7 +636,7 @@ def run_ours(args):
         return
     peak, peak_kind = measured_peak()
     achieved = agg["bytes"] / (ms / 1e3) / 1e9
-    traffic, _ = dram_traffic_per_launch(agg["lef_epochs"] / max(1, agg["launches"]))
+    traffic, tinfo = dram_traffic_per_launch(agg["lef_epochs"] / max(1, agg["launches"]))
     if batched is not None:
         bach = bbytes / (batched["ms"] / 1e3) / 1e9
         btraffic, _ = dram_traffic_per_launch(ble, "simulate_batch_kernel")
@@ -669,13 +671,18 @@ def run_ours(args):
                      "peak_source": f"{peak_kind} hbm_gbs", "kernel": "simulate_kernel",
                      "bytes_model": "24*LEF_epochs + 6*barriers*epochs + 8*contacts, summed over the "
                                     "launches of the timed region / region time (launches overlap)",
-                     "traffic_note": "DRAM bytes per launch: ncu bytes per LEF-epoch of one launch "
-                                     "run alone (profiles/simulate_kernel_traffic.json; ncu serialises "
-                                     "launches) x this run's LEF-epochs per launch; alone, a launch's "
-                                     "cells stay on chip and in L2, while 24 concurrent launches fill "
-                                     "every SM and spill L2 as the batched launch does"},
+                     "traffic_note": "DRAM bytes per launch: ncu bytes per LEF-epoch of one launch that "
+                                     "fills every SM with 24 KiB cells as the concurrent wave does "
+                                     "(profiles/simulate_kernel_traffic.json, 1064 resident cells of "
+                                     "chr11) x this run's LEF-epochs per launch",
+                     "traffic_over_algorithmic": None},
         "e2e": e2e, "clocks": clk, "batched": batched, "plain_serial": serial,
     }
+    if traffic is not None and agg["bytes"]:
+        line["roofline"]["traffic_over_algorithmic"] = traffic * agg["launches"] / agg["bytes"]
+        line["roofline"]["captured_launch_lef_epochs_per_s"] = tinfo.get("lef_epochs_per_s")
+    if batched is not None and batched["roofline"]["traffic"] is not None:
+        batched["roofline"]["traffic_over_algorithmic"] = batched["roofline"]["traffic"] / bbytes
     if batched is not None:
         line["batched"]["over_plain_wave_cells_per_s"] = batched["cells_per_s"] / line["cells_per_s"]
     if args.windows > 0:
