@@ -150,7 +150,10 @@ def run_windows(args, device, log):
     cells = 256
     wins = genome.batched_windows(seed=13, nwindows=args.windows, cells=cells)
     dev = torch.device("cuda", device)
+    from modlefork_gb300 import autotune
+
     with engine.Engine(genome.genome_config(), device) as eng:
+        autotune.apply_all(eng)
         tasks, bands, meta = [], {}, []
         for cfg, chrom, bars in wins:
             cid = eng.upload_chrom(chrom, bars)
@@ -212,6 +215,9 @@ def run_surrogate(args, log):
     from modlefork_gb300 import sweep
     from modlefork_gb300 import train_surrogate as T
 
+    from modlefork_gb300 import autotune
+
+    autotune.apply_all()
     net = T.load_weights(os.path.join(ROOT, "modlefork_gb300", "data", "surrogate_unet.npz"))
     n = args.sur_maps
     log(f"surrogate: simulating {n} fresh windows")
@@ -423,6 +429,7 @@ def run_ours(args):
 
         dist.init_process_group("nccl", init_method="env://")
     torch.cuda.set_device(local)
+    from modlefork_gb300 import autotune
     from modlefork_gb300 import build as mbuild
     from modlefork_gb300 import engine
     from modlefork_gb300.simulate import CONCURRENT_CARVEOUT, CONCURRENT_SMEM_BUDGET
@@ -561,6 +568,7 @@ def run_ours(args):
     if args.batched:
         w0 = workers[0]
         w0["eng"].set_debug_flags(0, 0)
+        tuning = autotune.apply_all(w0["eng"])
         btasks = [(w0["cids"][k], int(sd), int(tg), t["te"], t["nlefs"])
                   for k, t in enumerate(tasks) for sd, tg in zip(t["seeds"], t["targets"])]
         dbands = {w0["cids"][k]: t["d_band"].data_ptr() for k, t in enumerate(tasks)}
@@ -587,7 +595,9 @@ def run_ours(args):
         bdt = time.perf_counter() - t0
         batched = {"value": ble / (bms / 1e3), "unit": "LEF-epochs/s", "ms": bms, "launches": 1,
                    "cells_per_s": len(bst) / (bms / 1e3),
-                   "config": "the same 24 chromosomes x 512 cells in one batched launch, 16 KiB per cell, 60% carveout",
+                   "config": "the same 24 chromosomes x 512 cells in one batched launch, launch settings "
+                             + ("from the tuned table (modlefork_gb300/data/tuning_gb300.json)" if tuning
+                                else "16 KiB per cell, 60% carveout"),
                    "e2e": {"value": sum(x.lef_epochs for x in bst2) / bdt, "unit": "LEF-epochs/s",
                            "h2d_bytes_per_step": int(sum(b.nbytes for b in hb.values()) + len(btasks) * 40),
                            "d2h_bytes_per_step": int(sum(b.nbytes for b in hb.values()) + len(btasks) * 64)}}

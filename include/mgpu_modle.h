@@ -238,6 +238,22 @@ int mgpu_last_kernel_ms(mgpu_ctx* ctx, double* ms);
  * occupancy limit). */
 int mgpu_set_debug_flags(mgpu_ctx* ctx, uint32_t flags, uint64_t smem_budget);
 
+/* Tuned settings of large batched launches (no counterpart in the reference): entries in
+ * increasing max_lefs; a batch of at least 8 tasks per SM, on a context without explicit
+ * mgpu_set_debug_flags budget or carveout, takes the first entry whose max_lefs is at least the
+ * LEF count of its LEF-weighted median task (the last entry beyond).  smem_budget is the shared
+ * memory per cell (0 = the device limit), carveout_pct the shared-memory carveout preference
+ * (0 = the CUDA driver's default), max_cells_per_sm a cap on resident cells per SM (0 = the
+ * occupancy limit).  The settings move arrays between shared memory and global slots; results
+ * do not depend on them.  modlefork_gb300/autotune.py measures a table per device; n = 0 clears. */
+typedef struct mgpu_launch_setting {
+  uint64_t max_lefs;
+  uint64_t smem_budget;
+  uint32_t carveout_pct;
+  uint32_t max_cells_per_sm;
+} mgpu_launch_setting;
+int mgpu_set_launch_table(mgpu_ctx* ctx, const mgpu_launch_setting* table, uint64_t n);
+
 /* Profile of the last mgpu_simulate_cells or mgpu_simulate_batch launch made with debug flag
  * bit 4 (all zero otherwise; no counterpart in the reference): SM cycles
  * spent in each step of the epoch summed over cells (entries 0-15: burn-in, bind, rank,

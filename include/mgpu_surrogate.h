@@ -54,6 +54,14 @@ int msur_conv_forward(const void* x, int B, int L, int Cin, const void* w, int C
                       int act, void* out_pre, void* out_post, float* out_f32, int out_stride, int n_valid,
                       const void* gate, void* stream);
 
+/* Pipeline depth of msur_conv_forward for one N tile width (64, 128 or 256 output channels per
+ * tile, chosen by Cout): 2 to 4 shared-memory stages.  Fewer stages let 2-4 CTAs share an SM,
+ * so that one tile's epilogue overlaps another's main loop; the autotuner
+ * (modlefork_gb300/autotune.py) picks the depths per device.  Defaults 4 (64), 3 (128), 4 (256).
+ * msur_conv_get_stages returns the current depth (negative on a bad width). */
+int msur_conv_set_stages(int bn, int stages);
+int msur_conv_get_stages(int bn);
+
 /* Weight gradient of that convolution, ADDED to dw [Cout][taps][Cin] (FP32):
  *   dw[n][t][c] += sum_{b, l} dz[b, l, n] * x[b, l + t - (taps - 1) / 2, c]
  * taps 1 or 3; the position range is split over `splits` CTAs per tile (0 = enough to fill the

@@ -154,3 +154,9 @@ def make_barriers(barriers):
         arr[i].stp_inactive = float(b["stp_inactive"])
         arr[i].blocking_dir = int(b["blocking_dir"])
     return arr
+
+
+class LaunchSetting(C.Structure):
+    """mgpu_launch_setting: tuned settings of large batched launches."""
+    _fields_ = [("max_lefs", C.c_uint64), ("smem_budget", C.c_uint64), ("carveout_pct", C.c_uint32),
+                ("max_cells_per_sm", C.c_uint32)]

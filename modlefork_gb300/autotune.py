@@ -1,0 +1,188 @@
+"""Autotuner of the GPU paths' launch settings, measured on the device it runs on.
+
+  python -m modlefork_gb300.autotune [--out FILE] [--quick]
+
+1. Batched simulator, per cell-size bucket (LEFs per cell): for a synthetic chromosome of the
+   genome workload's kind with a typical LEF count of the bucket, one batched launch per
+   candidate (shared-memory budget per cell, shared-memory carveout, cap of resident cells per
+   SM), timed with CUDA events; the fastest in LEF-epochs/s becomes the bucket's entry of the
+   table that mgpu_set_launch_table installs.  The settings only move per-LEF arrays between
+   shared memory and global slots, so every candidate simulates the same cells.
+2. Surrogate convolutions: the pipeline depth (2-4 stages) per N tile width of
+   msur_conv_forward, by coordinate descent on the network's inference time at batch 256.
+
+The result is a JSON file keyed by the device's name and SM count; ``load_table`` and
+``apply_all`` read it back (engine contexts and the surrogate library take it from there).  The
+tuned table measured on a GB300 ships as modlefork_gb300/data/tuning_gb300.json.
+"""
+
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+DEFAULT_FILE = os.path.join(DATA, "tuning_gb300.json")
+
+# (bucket upper bound on LEFs per cell, chromosome length of its trial workload in bp at 20 LEFs/Mbp)
+BUCKETS = [(512, 16_000_000), (2048, 64_000_000), (4096, 160_000_000), (1 << 40, 250_000_000)]
+FULL = 1 << 30  # a budget above the device limit: as much shared memory per cell as a block may have
+CANDIDATES = [(FULL, 0, 0)] + [(kib * 1024, co, 0) for kib in (8, 12, 16, 24, 32, 48) for co in (60, 80, 100)]
+QUICK_CANDIDATES = [(FULL, 0, 0), (16384, 60, 0), (24576, 70, 0), (12288, 80, 0), (32768, 100, 0)]
+
+
+def log(msg):
+    print(f"[autotune {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
+def device_key():
+    import torch
+
+    p = torch.cuda.get_device_properties(0)
+    return f"{p.name}|{p.multi_processor_count}"
+
+
+def tune_simulator(candidates, cells, density=0.01, device=0):
+    import torch
+
+    from . import engine, genome
+
+    rng = np.random.default_rng(5)
+    table, trials = [], []
+    for max_lefs, length in BUCKETS:
+        cfg = genome.genome_config(target_contact_density=density, num_cells=cells)
+        chrom = engine.Chromosome(f"tune{length // 1000000}", length)
+        nb = int(round(length / 50_000))
+        recs = genome.bed_records(rng, length, nb, rng.beta(8.0, 2.0, size=nb))
+        bars = engine.barriers_from_bed(chrom, recs, cfg.barrier_occupied_stp, cfg.barrier_not_occupied_stp)
+        nl = engine.num_lefs(cfg, chrom.simulated_size)
+        tg, te = engine.task_targets(cfg, chrom.simulated_size, nl, cells)
+        nrows, ncols = engine.band_shape(cfg, chrom.simulated_size)
+        band = torch.zeros(nrows * ncols, dtype=torch.int32, device=f"cuda:{device}")
+        best = None
+        with engine.Engine(cfg, device) as eng:
+            cid = eng.upload_chrom(chrom, bars)
+            tasks = [(cid, engine.cell_seed(chrom.name, chrom.size, cfg.seed, i), int(tg[i]), te, nl)
+                     for i in range(cells)]
+            for budget, carveout, cap in candidates:
+                eng.set_debug_flags(((carveout & 0xFF) << 8) | ((cap & 0xFF) << 16), budget)
+                _, st = eng.simulate_batch(tasks, {cid: band.data_ptr()})
+                ms = eng.last_kernel_ms()
+                rate = sum(s.lef_epochs for s in st) / (ms / 1e3)
+                trials.append({"bucket_max_lefs": max_lefs, "lefs": nl, "smem_budget": budget,
+                               "carveout_pct": carveout, "max_cells_per_sm": cap, "ms": ms, "lef_epochs_per_s": rate})
+                log(f"{nl} LEFs: budget {min(budget, 1 << 20) // 1024} KiB, carveout {carveout} %, cap {cap}: "
+                    f"{rate:.3e} LEF-epochs/s")
+                if best is None or rate > best[0]:
+                    best = (rate, budget, carveout, cap)
+        table.append({"max_lefs": max_lefs, "smem_budget": best[1], "carveout_pct": best[2],
+                      "max_cells_per_sm": best[3], "lef_epochs_per_s": best[0], "trial_lefs": nl})
+    return table, trials
+
+
+def tune_surrogate(batch=256, reps=5):
+    import torch
+
+    from . import surrogate as S
+    from . import surrogate_ops as ops
+
+    net = S.UNet(seed=0)
+    x = torch.zeros(batch, net.length, S.IN_CH, dtype=torch.bfloat16, device=net.dev)
+    x[:, :, :8].normal_()
+
+    def timed():
+        net.forward(x)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(reps):
+            net.forward(x)
+        ev1.record()
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / reps
+
+    choice = {bn: ops.conv_get_stages(bn) for bn in (64, 128, 256)}
+    trials = []
+    base = timed()
+    for _ in range(2):  # two rounds of coordinate descent
+        for bn in (256, 128, 64):
+            times = {}
+            for stages in (2, 3, 4):
+                ops.conv_set_stages(bn, stages)
+                times[stages] = timed()
+                trials.append({"bn": bn, "stages": stages, "others": dict(choice), "ms_per_batch": times[stages]})
+            choice[bn] = min(times, key=times.get)
+            ops.conv_set_stages(bn, choice[bn])
+            log(f"conv N tile {bn}: {times} -> {choice[bn]} stages")
+    best = timed()
+    return {"stages": {str(k): v for k, v in choice.items()}, "ms_per_batch_default": base,
+            "ms_per_batch_tuned": best, "batch": batch}, trials
+
+
+def load_table(path=DEFAULT_FILE):
+    """The tuned settings for the current device, or None when the file has none for it."""
+    if not os.path.exists(path):
+        return None
+    try:
+        d = json.load(open(path))
+        return d.get("devices", {}).get(device_key())
+    except (OSError, ValueError):
+        return None
+
+
+def apply_engine(eng, tuned):
+    """Install the simulator table of `tuned` (load_table's result) on an engine context."""
+    if tuned and tuned.get("simulator"):
+        eng.set_launch_table([(e["max_lefs"], e["smem_budget"], e["carveout_pct"], e["max_cells_per_sm"])
+                              for e in tuned["simulator"]])
+
+
+def apply_all(eng=None, path=DEFAULT_FILE):
+    """Apply the shipped tuning for this device (if it has any) to an engine and the surrogate
+    library; returns the settings applied or None."""
+    tuned = load_table(path)
+    if tuned:
+        if eng is not None:
+            apply_engine(eng, tuned)
+        apply_surrogate(tuned)
+    return tuned
+
+
+def apply_surrogate(tuned):
+    """Set the convolution pipeline depths of `tuned` in the surrogate library."""
+    from . import surrogate_ops as ops
+
+    if tuned and tuned.get("surrogate"):
+        for bn, stages in tuned["surrogate"]["stages"].items():
+            ops.conv_set_stages(int(bn), int(stages))
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--out", default="tuning.json")
+    ap.add_argument("--quick", action="store_true", help="five simulator candidates instead of nineteen")
+    ap.add_argument("--cells", type=int, default=1600)
+    args = ap.parse_args(argv)
+    from . import build
+
+    build.build()
+    cands = QUICK_CANDIDATES if args.quick else CANDIDATES
+    sim_table, sim_trials = tune_simulator(cands, args.cells)
+    sur, sur_trials = tune_surrogate()
+    entry = {"simulator": sim_table, "surrogate": sur, "measured": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime()),
+             "trials": {"simulator": sim_trials, "surrogate": sur_trials},
+             "command": "python -m modlefork_gb300.autotune" + (" --quick" if args.quick else "")}
+    out = {"devices": {}}
+    if os.path.exists(args.out):
+        out = json.load(open(args.out))
+    out.setdefault("devices", {})[device_key()] = entry
+    with open(args.out, "w") as f:
+        json.dump(out, f, indent=1)
+    print(json.dumps({"device": device_key(), "simulator": sim_table, "surrogate": sur}))
+
+
+if __name__ == "__main__":
+    main()

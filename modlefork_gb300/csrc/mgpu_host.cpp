@@ -565,6 +565,7 @@ struct mgpu_ctx {
   uint64_t* d_prof = nullptr;  // profile counters of the last launch
   uint64_t h_prof[32] = {0};
   void* noalloc_scratch = nullptr;  // device address of the fixed scratch, looked up by this context
+  std::vector<mgpu_launch_setting> launch_table;  // tuned settings of large batched launches
 };
 
 extern "C" const char* mgpu_last_error_string(void) { return g_last_error.c_str(); }
@@ -860,6 +861,21 @@ extern "C" int mgpu_last_profile(mgpu_ctx* ctx, uint64_t counters[32]) {
   return MGPU_OK;
 }
 
+extern "C" int mgpu_set_launch_table(mgpu_ctx* ctx, const mgpu_launch_setting* table, uint64_t n) {
+  if (!ctx || (n && !table)) return fail(MGPU_ERR_INVALID_ARG, "mgpu_set_launch_table: null argument");
+  std::vector<mgpu_launch_setting> t(table, table + n);
+  for (uint64_t i = 0; i < n; ++i) {
+    if (t[i].carveout_pct > 100 || t[i].max_cells_per_sm > 255)
+      return fail(MGPU_ERR_INVALID_ARG, "mgpu_set_launch_table: entry %llu: carveout above 100 %% or cap above 255",
+                  (unsigned long long)i);
+    if (i && t[i].max_lefs <= t[i - 1].max_lefs)
+      return fail(MGPU_ERR_INVALID_ARG, "mgpu_set_launch_table: max_lefs must increase");
+  }
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->launch_table = std::move(t);
+  return MGPU_OK;
+}
+
 extern "C" int mgpu_set_debug_flags(mgpu_ctx* ctx, uint32_t flags, uint64_t smem_budget) {
   if (!ctx) return fail(MGPU_ERR_INVALID_ARG, "mgpu_set_debug_flags: null context");
   std::lock_guard<std::mutex> lk(ctx->mu);
@@ -1114,7 +1130,32 @@ extern "C" int mgpu_simulate_batch(mgpu_ctx* ctx, const mgpu_batch_task* tasks, 
   // an SM and the per-LEF arrays that live in global slots keep an 88 KB L1 (measured best on the
   // genome workload).
   const bool large = ntasks >= 8ull * (uint64_t)dev_sms;
-  const uint64_t budget = ctx->smem_budget ? ctx->smem_budget : (large ? 16384ull : 0ull);
+  uint64_t budget = ctx->smem_budget ? ctx->smem_budget : (large ? 16384ull : 0ull);
+  // a tuned table (mgpu_set_launch_table) replaces those defaults for large batches without
+  // explicit switches: the entry of the LEF-weighted median cell's LEF count
+  const mgpu_launch_setting* tuned = nullptr;
+  if (large && !ctx->smem_budget && !(ctx->debug_flags & 0xFFFF00u) && !ctx->launch_table.empty()) {
+    std::vector<uint64_t> nl(ntasks);
+    uint64_t total = 0;
+    for (uint64_t i = 0; i < ntasks; ++i) total += (nl[i] = tasks[i].num_lefs);
+    std::sort(nl.begin(), nl.end());
+    uint64_t acc = 0, median = nl.back();
+    for (uint64_t v : nl) {
+      acc += v;
+      if (2 * acc >= total) {
+        median = v;
+        break;
+      }
+    }
+    tuned = &ctx->launch_table.back();
+    for (const mgpu_launch_setting& e : ctx->launch_table) {
+      if (median <= e.max_lefs) {
+        tuned = &e;
+        break;
+      }
+    }
+    budget = tuned->smem_budget;
+  }
   std::vector<BatchPlan> plans(keys.size());
   u32 smem_bytes = 0;
   u64 slot_bytes = 0;
@@ -1169,8 +1210,12 @@ extern "C" int mgpu_simulate_batch(mgpu_ctx* ctx, const mgpu_batch_task* tasks, 
   CK(cudaMemcpyAsync(d_tasks.p, bt.data(), ntasks * sizeof(BatchTask), cudaMemcpyHostToDevice, st));
   // tuning switches (mgpu_set_debug_flags bits 8-15: carveout percent, 16-23: blocks per SM cap)
   u32 carveout = (ctx->debug_flags >> 8) & 0xFFu;
-  const u32 max_per_sm = (ctx->debug_flags >> 16) & 0xFFu;
+  u32 max_per_sm = (ctx->debug_flags >> 16) & 0xFFu;
   if (!carveout && large && !ctx->smem_budget) carveout = 60;
+  if (tuned) {
+    carveout = tuned->carveout_pct;
+    max_per_sm = tuned->max_cells_per_sm;
+  }
   if (slot_bytes) {
     KParams Pslot = plans[0].P;
     Pslot.slot_bytes = slot_bytes;

@@ -429,6 +429,101 @@ __global__ void upcat_bwd_kernel(const bf16* dcat, const bf16* z, int B, int Lh,
   }
 }
 
+// ---- the same steps eight channels (16 bytes) per thread, for channel counts, strides and
+// offsets that are multiples of 8 and 16-byte aligned buffers (every shape of the network)
+__device__ __forceinline__ void ld8(const bf16* p, float (&f)[8]) {
+  const uint4 u = *reinterpret_cast<const uint4*>(p);
+  const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162*>(&w[k]);
+    f[2 * k] = __low2float(h);
+    f[2 * k + 1] = __high2float(h);
+  }
+}
+__device__ __forceinline__ void st8(bf16* p, const float (&f)[8]) {
+  uint32_t w[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+    w[k] = *reinterpret_cast<const uint32_t*>(&h);
+  }
+  *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+__global__ void pool2_v8_kernel(const bf16* x, int B, int Lout, int C, bf16* y) {
+  const int C8 = C / 8;
+  const size_t n = static_cast<size_t>(B) * Lout * C8;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = static_cast<int>(i % C8) * 8;
+    const size_t bl = i / C8;  // b * Lout + l
+    const size_t src = 2 * bl * C + c;  // row 2l of sequence b: (b * 2 Lout + 2 l) * C
+    float a[8], b[8];
+    ld8(x + src, a);
+    ld8(x + src + C, b);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = 0.5f * (a[k] + b[k]);
+    st8(y + bl * C + c, a);
+  }
+}
+
+__global__ void skip_grad_v8_kernel(const bf16* dpool, int Lp, const bf16* dcat, int cat_stride, int cat_off,
+                                    const bf16* z, int B, int L, int C, bf16* dz) {
+  const int C8 = C / 8;
+  const size_t n = static_cast<size_t>(B) * L * C8;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = static_cast<int>(i % C8) * 8;
+    const size_t bl = i / C8;
+    const int l = bl % L;
+    const int b = bl / L;
+    float g[8] = {0, 0, 0, 0, 0, 0, 0, 0}, t[8];
+    if (dpool && l / 2 < Lp) {
+      ld8(dpool + (static_cast<size_t>(b) * Lp + l / 2) * C + c, t);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) g[k] += 0.5f * t[k];
+    }
+    if (dcat) {
+      ld8(dcat + bl * cat_stride + cat_off + c, t);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) g[k] += t[k];
+    }
+    ld8(z + bl * C + c, t);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) g[k] *= dsilu(t[k]);
+    st8(dz + bl * C + c, g);
+  }
+}
+
+__global__ void upcat_v8_kernel(const bf16* x, const bf16* skip, int B, int L, int C1, int C2, bf16* out) {
+  const int C = C1 + C2, C8 = C / 8;
+  const size_t n = static_cast<size_t>(B) * L * C8;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = static_cast<int>(i % C8) * 8;
+    const size_t bl = i / C8;
+    const int l = bl % L;
+    const int b = bl / L;
+    const bf16* src = c < C1 ? x + (static_cast<size_t>(b) * (L / 2) + l / 2) * C1 + c : skip + bl * C2 + (c - C1);
+    *reinterpret_cast<uint4*>(out + bl * C + c) = *reinterpret_cast<const uint4*>(src);
+  }
+}
+
+__global__ void upcat_bwd_v8_kernel(const bf16* dcat, const bf16* z, int B, int Lh, int C1, int C, bf16* dz) {
+  const int C8 = C1 / 8;
+  const size_t n = static_cast<size_t>(B) * Lh * C8;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = static_cast<int>(i % C8) * 8;
+    const size_t bl = i / C8;  // b * Lh + l
+    const size_t r = 2 * bl;   // row 2l of sequence b in dcat
+    float a[8], b[8], t[8];
+    ld8(dcat + r * C + c, a);
+    ld8(dcat + (r + 1) * C + c, b);
+    ld8(z + bl * C1 + c, t);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = (a[k] + b[k]) * dsilu(t[k]);
+    st8(dz + bl * C1 + c, a);
+  }
+}
+
 // db[c] += sum over rows of dz[r * stride + c], c < C; one block column of 32 channels per block
 __global__ void bias_grad_kernel(const bf16* dz, size_t rows, int C, int stride, float* db) {
   const int c = blockIdx.x * 32 + threadIdx.x;
@@ -588,6 +683,9 @@ thread_local char g_err[512];
 std::mutex g_mu;
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 unsigned* g_dev_err[64] = {};
+// pipeline stages of the forward/data-gradient convolution per N tile width (64, 128, 256):
+// fewer stages let more CTAs share an SM, so one tile's epilogue overlaps another's main loop
+int g_conv_stages[3] = {4, 3, 4};
 
 int fail(int code, const char* fmt, ...) {
   va_list ap;
@@ -734,9 +832,33 @@ int msur_conv_forward(const void* x, int B, int L, int Cin, const void* w, int C
   a.err = err;
   const int ntn = (Cout + BN - 1) / BN;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (BN == 256) return launch_conv<256, 4>(a, ntn, st);
-  if (BN == 128) return launch_conv<128, 3>(a, ntn, st);
+  const int stages = g_conv_stages[BN == 256 ? 2 : (BN == 128 ? 1 : 0)];
+  if (BN == 256) {
+    if (stages == 2) return launch_conv<256, 2>(a, ntn, st);
+    if (stages == 3) return launch_conv<256, 3>(a, ntn, st);
+    return launch_conv<256, 4>(a, ntn, st);
+  }
+  if (BN == 128) {
+    if (stages == 2) return launch_conv<128, 2>(a, ntn, st);
+    if (stages == 4) return launch_conv<128, 4>(a, ntn, st);
+    return launch_conv<128, 3>(a, ntn, st);
+  }
+  if (stages == 2) return launch_conv<64, 2>(a, ntn, st);
+  if (stages == 3) return launch_conv<64, 3>(a, ntn, st);
   return launch_conv<64, 4>(a, ntn, st);
+}
+
+int msur_conv_set_stages(int bn, int stages) {
+  if ((bn != 64 && bn != 128 && bn != 256) || stages < 2 || stages > 4)
+    return fail(MSUR_ERR_INVALID_ARG, "msur_conv_set_stages: N tile 64, 128 or 256 and 2 to 4 stages");
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_conv_stages[bn == 256 ? 2 : (bn == 128 ? 1 : 0)] = stages;
+  return MSUR_OK;
+}
+
+int msur_conv_get_stages(int bn) {
+  if (bn != 64 && bn != 128 && bn != 256) return fail(MSUR_ERR_INVALID_ARG, "msur_conv_get_stages: bad N tile");
+  return g_conv_stages[bn == 256 ? 2 : (bn == 128 ? 1 : 0)];
 }
 
 int msur_conv_wgrad(const void* x, const void* dz, int B, int L, int Cin, int Cout, int taps, float* dw, int splits,
@@ -785,6 +907,11 @@ int msur_conv_wgrad(const void* x, const void* dz, int B, int L, int Cin, int Co
 int msur_pool2(const void* x, int B, int Lout, int C, void* y, void* stream) {
   if (!x || !y || B <= 0 || Lout <= 0 || C <= 0) return fail(MSUR_ERR_INVALID_ARG, "msur_pool2: bad argument");
   const size_t n = static_cast<size_t>(B) * Lout * C;
+  if (C % 8 == 0 && aligned16(x) && aligned16(y)) {
+    pool2_v8_kernel<<<grid_for(n / 8), 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const bf16*>(x), B,
+                                                                                   Lout, C, static_cast<bf16*>(y));
+    return cuda_ok(cudaGetLastError(), "pool2_v8_kernel launch");
+  }
   pool2_kernel<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const bf16*>(x), B, Lout, C,
                                                                            static_cast<bf16*>(y));
   return cuda_ok(cudaGetLastError(), "pool2_kernel launch");
@@ -794,6 +921,13 @@ int msur_skip_grad(const void* dpool, int Lp, const void* dcat, int cat_stride, 
                    int L, int C, void* dz, void* stream) {
   if (!z || !dz || B <= 0 || L <= 0 || C <= 0) return fail(MSUR_ERR_INVALID_ARG, "msur_skip_grad: bad argument");
   const size_t n = static_cast<size_t>(B) * L * C;
+  if (C % 8 == 0 && cat_stride % 8 == 0 && cat_off % 8 == 0 && aligned16(z) && aligned16(dz) &&
+      (!dpool || aligned16(dpool)) && (!dcat || aligned16(dcat))) {
+    skip_grad_v8_kernel<<<grid_for(n / 8), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(dpool), Lp, static_cast<const bf16*>(dcat), cat_stride, cat_off,
+        static_cast<const bf16*>(z), B, L, C, static_cast<bf16*>(dz));
+    return cuda_ok(cudaGetLastError(), "skip_grad_v8_kernel launch");
+  }
   skip_grad_kernel<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
       static_cast<const bf16*>(dpool), Lp, static_cast<const bf16*>(dcat), cat_stride, cat_off,
       static_cast<const bf16*>(z), B, L, C, static_cast<bf16*>(dz));
@@ -803,6 +937,11 @@ int msur_skip_grad(const void* dpool, int Lp, const void* dcat, int cat_stride, 
 int msur_upcat(const void* x, const void* skip, int B, int L, int C1, int C2, void* out, void* stream) {
   if (!x || !skip || !out || B <= 0 || L <= 0 || (L % 2)) return fail(MSUR_ERR_INVALID_ARG, "msur_upcat: bad argument");
   const size_t n = static_cast<size_t>(B) * L * (C1 + C2);
+  if (C1 % 8 == 0 && C2 % 8 == 0 && aligned16(x) && aligned16(skip) && aligned16(out)) {
+    upcat_v8_kernel<<<grid_for(n / 8), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(x), static_cast<const bf16*>(skip), B, L, C1, C2, static_cast<bf16*>(out));
+    return cuda_ok(cudaGetLastError(), "upcat_v8_kernel launch");
+  }
   upcat_kernel<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
       static_cast<const bf16*>(x), static_cast<const bf16*>(skip), B, L, C1, C2, static_cast<bf16*>(out));
   return cuda_ok(cudaGetLastError(), "upcat_kernel launch");
@@ -811,6 +950,11 @@ int msur_upcat(const void* x, const void* skip, int B, int L, int C1, int C2, vo
 int msur_upcat_bwd(const void* dcat, const void* z, int B, int Lh, int C1, int C, void* dz, void* stream) {
   if (!dcat || !z || !dz || B <= 0 || Lh <= 0 || C1 > C) return fail(MSUR_ERR_INVALID_ARG, "msur_upcat_bwd: bad argument");
   const size_t n = static_cast<size_t>(B) * Lh * C1;
+  if (C1 % 8 == 0 && C % 8 == 0 && aligned16(dcat) && aligned16(z) && aligned16(dz)) {
+    upcat_bwd_v8_kernel<<<grid_for(n / 8), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const bf16*>(dcat), static_cast<const bf16*>(z), B, Lh, C1, C, static_cast<bf16*>(dz));
+    return cuda_ok(cudaGetLastError(), "upcat_bwd_v8_kernel launch");
+  }
   upcat_bwd_kernel<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
       static_cast<const bf16*>(dcat), static_cast<const bf16*>(z), B, Lh, C1, C, static_cast<bf16*>(dz));
   return cuda_ok(cudaGetLastError(), "upcat_bwd_kernel launch");

@@ -76,6 +76,7 @@ def load(path=LIB_PATH):
         "mgpu_last_kernel_ms": (i32, [C.c_void_p, P(C.c_double)]),
         "mgpu_set_debug_flags": (i32, [C.c_void_p, C.c_uint32, u64]),
         "mgpu_last_profile": (i32, [C.c_void_p, P(u64)]),
+        "mgpu_set_launch_table": (i32, [C.c_void_p, P(abi.LaunchSetting), u64]),
         "mgpu_probe_samplers": (i32, [i32, i32, C.c_void_p, u64, u64, C.c_double, C.c_double, C.c_void_p,
                                       C.c_void_p]),
         "mgpu_probe_libm": (i32, [i32, i32, C.c_void_p, C.c_void_p, u64, C.c_double, C.c_double, C.c_double,
@@ -421,6 +422,14 @@ class Engine:
         ms = C.c_double()
         _check(self.lib.mgpu_last_kernel_ms(self.h, C.byref(ms)), "mgpu_last_kernel_ms")
         return ms.value
+
+    def set_launch_table(self, entries):
+        """Tuned settings of large batched launches: entries (max_lefs, smem_budget, carveout_pct,
+        max_cells_per_sm) in increasing max_lefs; an empty list clears the table."""
+        arr = (abi.LaunchSetting * max(1, len(entries)))()
+        for i, (ml, sb, co, mx) in enumerate(entries):
+            arr[i] = abi.LaunchSetting(int(ml), int(sb), int(co), int(mx))
+        _check(self.lib.mgpu_set_launch_table(self.h, arr, len(entries)), "mgpu_set_launch_table")
 
     def set_debug_flags(self, flags=0, smem_budget=0):
         """Force the serial restatement of some steps (bit 0 rank, 1 adjust, 2 collisions,

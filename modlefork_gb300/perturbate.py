@@ -144,7 +144,10 @@ def run_windows(cfg, planned, device=0):
     task, mgpu_simulate_batch); returns one WindowResult per task, in the given order."""
     if not planned:
         return []
+    from . import autotune
+
     with engine.Engine(cfg, device) as eng:
+        autotune.apply_all(eng)
         batch, bands, cids = [], {}, []
         for chrom, t in planned:
             cid = eng.upload_window(chrom, t["window"][0], t["window"][1], t["barriers"])

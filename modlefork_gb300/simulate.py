@@ -120,7 +120,10 @@ def simulate_genome_batched(cfg, genome, ncells=None, device=0, simulate_wo_barr
     Same results as one launch per chromosome."""
     ncells = int(cfg.num_cells if ncells is None else ncells)
     jobs = [(c, b) for c, b in genome if b or simulate_wo_barriers]
+    from . import autotune
+
     with engine.Engine(cfg, device) as eng:
+        autotune.apply_all(eng)
         preps, tasks, bands = [], [], {}
         for chrom, barriers in jobs:
             t = prepare_chrom(eng, cfg, chrom, barriers, ncells)

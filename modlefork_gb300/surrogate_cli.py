@@ -15,7 +15,7 @@ import os
 import numpy as np
 import torch
 
-from . import build
+from . import autotune, build
 from . import surrogate as S
 from . import sweep
 from . import train_surrogate as T
@@ -32,6 +32,7 @@ def main(argv=None):
     ap.add_argument("--out", default=None)
     args = ap.parse_args(argv)
     build.build()
+    autotune.apply_all()
     net = T.load_weights(args.weights)
     wins = [sweep.window(k, cells=1, density=1.0) for k in range(args.first, args.first + args.batch)]
     track = torch.from_numpy(np.stack([w[3] for w in wins])).to(net.dev)

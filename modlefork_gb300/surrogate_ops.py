@@ -46,6 +46,8 @@ def load(path=LIB_PATH):
         "msur_band_target": (i32, [vp, u64, i32, vp, vp]),
         "msur_map_sums": (i32, [vp, u64, vp, u64, u64, i32, vp, vp, vp]),
         "msur_compact_rows": (i32, [vp, i32, u64, i32, vp, vp]),
+        "msur_conv_set_stages": (i32, [i32, i32]),
+        "msur_conv_get_stages": (i32, [i32]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(lib, name)
@@ -184,3 +186,12 @@ def map_scores(pred, ref, n, nmaps, pstride=None, rstride=None):
 def compact_rows(inp, n_valid, out):
     rows = inp.numel() // inp.shape[-1]
     _check(load().msur_compact_rows(_p(inp), inp.shape[-1], rows, n_valid, _p(out), _stream()), "msur_compact_rows")
+
+
+def conv_set_stages(bn, stages):
+    """Pipeline depth (2-4 stages) of the convolution kernels with N tile bn (64, 128, 256)."""
+    _check(load().msur_conv_set_stages(bn, stages), "msur_conv_set_stages")
+
+
+def conv_get_stages(bn):
+    return load().msur_conv_get_stages(bn)

@@ -104,7 +104,10 @@ def simulate_sets(ks, seed=2024, cells=1024, density=10.0, device=0, smem_budget
     dev = torch.device("cuda", device)
     wins = [window(k, seed, cells, density) for k in ks]
     targets = torch.empty(len(ks), NCOLS, NROWS, dtype=torch.float32, device=dev)
+    from . import autotune
+
     with engine.Engine(genome.genome_config(), device) as eng:
+        autotune.apply_all(eng)
         if smem_budget is not None:
             eng.set_debug_flags(0, smem_budget)
         tasks, bands = [], {}

@@ -100,6 +100,9 @@ def main(argv=None):
     from . import build
 
     build.build()
+    from . import autotune
+
+    autotune.apply_all()
     os.makedirs(args.out, exist_ok=True)
     dev = torch.device("cuda", 0)
     report = {"config": vars(args)}

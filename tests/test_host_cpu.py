@@ -160,3 +160,23 @@ def test_batched_windows_follow_the_workload_ranges(lib):
     assert bden.min() > 4.0 and bden.max() < 41.0
     for cfg, chrom, bars in wins[:5]:
         assert cfg.num_cells == 4 and np.isclose(cfg.rev_extrusion_speed, 0.8 * cfg.bin_size)
+
+
+def test_launch_setting_layout_and_surrogate_library_exports():
+    assert C.sizeof(abi.LaunchSetting) == 24
+    from modlefork_gb300 import surrogate_ops
+
+    slib = surrogate_ops.load()
+    text = open(os.path.join(ROOT, "include", "mgpu_surrogate.h")).read()
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    names = sorted(set(re.findall(r"\b(msur_[a-z0-9_]+)\s*\(", text)))
+    assert len(names) >= 15
+    missing = [n for n in names if not hasattr(slib, n)]
+    assert not missing, missing
+    # argument checks that run before any device work
+    with pytest.raises(surrogate_ops.SurrogateKernelError):
+        surrogate_ops.conv_set_stages(96, 2)
+    with pytest.raises(surrogate_ops.SurrogateKernelError):
+        surrogate_ops.conv_set_stages(128, 5)
+    for bn, default in ((64, 4), (128, 3), (256, 4)):
+        assert surrogate_ops.conv_get_stages(bn) == default
