@@ -30,7 +30,7 @@ DEFAULT_FILE = os.path.join(DATA, "tuning_gb300.json")
 # (bucket upper bound on LEFs per cell, chromosome length of its trial workload in bp at 20 LEFs/Mbp)
 BUCKETS = [(512, 16_000_000), (2048, 64_000_000), (4096, 160_000_000), (1 << 40, 250_000_000)]
 FULL = 1 << 30  # a budget above the device limit: as much shared memory per cell as a block may have
-CANDIDATES = [(FULL, 0, 0)] + [(kib * 1024, co, 0) for kib in (8, 12, 16, 24, 32, 48) for co in (60, 80, 100)]
+CANDIDATES = [(FULL, 0, 0)] + [(kib * 1024, co, 0) for kib in (12, 16, 20, 24, 32, 48) for co in (60, 80, 100)]
 QUICK_CANDIDATES = [(FULL, 0, 0), (16384, 60, 0), (24576, 70, 0), (12288, 80, 0), (32768, 100, 0)]
 
 
@@ -69,7 +69,11 @@ def tune_simulator(candidates, cells, density=0.01, device=0):
                      for i in range(cells)]
             for budget, carveout, cap in candidates:
                 eng.set_debug_flags(((carveout & 0xFF) << 8) | ((cap & 0xFF) << 16), budget)
-                _, st = eng.simulate_batch(tasks, {cid: band.data_ptr()})
+                try:
+                    _, st = eng.simulate_batch(tasks, {cid: band.data_ptr()})
+                except engine.EngineError as e:  # a budget below the cell's fixed shared memory
+                    log(f"{nl} LEFs: budget {budget // 1024} KiB rejected ({e})")
+                    continue
                 ms = eng.last_kernel_ms()
                 rate = sum(s.lef_epochs for s in st) / (ms / 1e3)
                 trials.append({"bucket_max_lefs": max_lefs, "lefs": nl, "smem_budget": budget,
