@@ -366,19 +366,63 @@ def write_bedpe(path, lines, header=True):
             f.write(ln + "\n")
 
 
+def reference_bands(cfg, genome, device=0, world=1, rank=0, group=None):
+    """The reference run of simulate_window's comparison: every chromosome's band over all
+    cells.  With several ranks each simulates its contiguous range of cell ids and the bands are
+    summed exactly over the ranks (sharding.allreduce_band_)."""
+    import torch
+
+    from . import sharding
+    from .simulate import simulate_genome_batched
+
+    lo, hi = sharding.cell_range(int(cfg.num_cells), world, rank)
+    res = simulate_genome_batched(cfg, genome, device=device, cell_range=(lo, hi))
+    bands = {r.chrom.name: r.band for r in res}
+    if world > 1:
+        dev = torch.device("cuda", device) if torch.cuda.is_available() else torch.device("cpu")
+        for name, b in bands.items():
+            t = torch.from_numpy(b.view(np.int32)).to(dev)
+            bands[name] = sharding.allreduce_band_(t, group).cpu().numpy().view(np.uint32)
+    return bands
+
+
+def run(cfg, g, feats1, feats2, deletion_size=10_000, deletion_list=None, block_size=9, max_tasks=None, device=0,
+        world=1, rank=0, group=None, reference=None, windows_fn=None):
+    """The command's work on one rank: the reference bands, the planned (window, deletion) cells
+    (every rank plans the same queue), this rank's block of the queue simulated and scored, and
+    the records of all ranks in task-id order (every rank returns them).  ``reference(cfg, g)``
+    and ``windows_fn(cfg, planned)`` replace the GPU's reference run and window launch (tests run
+    them with the oracle)."""
+    from . import sharding
+
+    names = {c.name for c, _ in g}
+    features = {n: ([(f[1], f[2]) for f in feats1[n]], [(f[1], f[2]) for f in feats2[n]])
+                for n in names if n in feats1 and n in feats2}
+    ref = reference(cfg, g) if reference else reference_bands(cfg, g, device, world, rank, group)
+    dels = read_bed_intervals(deletion_list) if deletion_list else None
+    planned = plan_windows(cfg, g, deletion_size, features, max_tasks, dels)
+    win = windows_fn or (lambda c, p: run_windows(c, p, device=device))
+    if world == 1:
+        return perturbate_records(cfg, feats1, feats2, ref, win(cfg, planned), block_size), len(planned)
+    return sharding.perturbate_sharded(cfg, planned, feats1, feats2, ref, world, rank, win, block_size,
+                                       group), len(planned)
+
+
 def _main(argv=None):
     """modle perturbate on a generated workload: a reference run of the whole genome, then one
     cell per (window, deletion) in one batched launch, scored for every pair of features of the
-    two BED files.  Example:
+    two BED files.  Under torchrun (WORLD_SIZE > 1) every rank simulates its share of the
+    reference cells and a contiguous block of the window queue on GPU LOCAL_RANK; rank 0 writes
+    the bedpe.  Example:
 
     python -m modlefork_gb300.perturbate --workload parity --features a.bed b.bed --out x.bedpe.gz
     """
     import argparse
     import json
+    import os
     import time
 
     from . import genome as gen
-    from .simulate import simulate_genome_batched
 
     ap = argparse.ArgumentParser(description=_main.__doc__)
     ap.add_argument("--workload", choices=["parity", "genome"], default="parity")
@@ -395,22 +439,28 @@ def _main(argv=None):
     args = ap.parse_args(argv)
     if args.block_size < 1 or args.block_size % 2 == 0:
         ap.error("--block-size must be a positive odd number")
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    device = int(os.environ.get("LOCAL_RANK", args.device)) if world > 1 else args.device
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(device)
+        dist.init_process_group("nccl", init_method="env://")
     cfg, g = gen.parity_10mbp() if args.workload == "parity" else gen.genome_24chr(nchroms=args.chroms)
     feats1, feats2 = read_bed_features(args.features[0]), read_bed_features(args.features[1])
-    names = {c.name for c, _ in g}
-    features = {n: ([(f[1], f[2]) for f in feats1[n]], [(f[1], f[2]) for f in feats2[n]])
-                for n in names if n in feats1 and n in feats2}
     t0 = time.perf_counter()
-    ref = {r.chrom.name: r.band for r in simulate_genome_batched(cfg, g, device=args.device)}
-    t1 = time.perf_counter()
-    dels = read_bed_intervals(args.deletion_list) if args.deletion_list else None
-    results = run_windows(cfg, plan_windows(cfg, g, args.deletion_size, features, args.max_tasks, dels),
-                          device=args.device)
-    t2 = time.perf_counter()
-    lines = perturbate_records(cfg, feats1, feats2, ref, results, args.block_size)
-    write_bedpe(args.out, lines, header=not args.no_header)
-    print(json.dumps({"workload": args.workload, "tasks": len(results), "records": len(lines),
-                      "reference_s": t1 - t0, "windows_s": t2 - t1, "scoring_s": time.perf_counter() - t2}))
+    lines, ntasks = run(cfg, g, feats1, feats2, args.deletion_size, args.deletion_list, args.block_size,
+                        args.max_tasks, device, world, rank)
+    if rank == 0:
+        write_bedpe(args.out, lines, header=not args.no_header)
+        print(json.dumps({"workload": args.workload, "tasks": ntasks, "records": len(lines), "ranks": world,
+                          "seconds": time.perf_counter() - t0}))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
 
 
 if __name__ == "__main__":

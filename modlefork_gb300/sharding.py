@@ -43,6 +43,20 @@ def allreduce_counts(values, device=None, group=None):
     return out.astype(a.dtype)
 
 
+def allreduce_band_(band, group=None):
+    """In-place exact sum over ranks of a uint32 band held as an int32 tensor (on the GPU with
+    NCCL, on the CPU with gloo): two's-complement int32 addition wraps exactly as uint32
+    addition does, so the result is the uint32 sum modulo 2^32, the reference's contacts_t
+    arithmetic, without a round trip through host memory."""
+    import torch
+    import torch.distributed as dist
+
+    if band.dtype != torch.int32:
+        raise TypeError("the band must be an int32 view of the uint32 counts")
+    dist.all_reduce(band, op=dist.ReduceOp.SUM, group=group)
+    return band
+
+
 def reduce_timing(ms, counters, device=None, group=None):
     """Max of the ranks' timed-region lengths and sums of their counters (dict of numbers)."""
     import torch

@@ -114,11 +114,14 @@ def simulate_genome(cfg, genome, ncells=None, device=0, simulate_wo_barriers=Fal
         raise errors[0]
     return [results[i] for i, _, _ in jobs]
 
-def simulate_genome_batched(cfg, genome, ncells=None, device=0, simulate_wo_barriers=False):
+def simulate_genome_batched(cfg, genome, ncells=None, device=0, simulate_wo_barriers=False, cell_range=None):
     """simulate_genome with every chromosome's cells in one batched launch (mgpu_simulate_batch):
     one persistent kernel and one work queue for the whole genome, largest chromosomes first.
-    Same results as one launch per chromosome."""
+    Same results as one launch per chromosome.  cell_range = (lo, hi) simulates only cell ids
+    lo .. hi - 1 of each chromosome (one rank's share); their seeds and targets are those of the
+    full run."""
     ncells = int(cfg.num_cells if ncells is None else ncells)
+    lo, hi = cell_range if cell_range is not None else (0, ncells)
     jobs = [(c, b) for c, b in genome if b or simulate_wo_barriers]
     from . import autotune
 
@@ -129,13 +132,13 @@ def simulate_genome_batched(cfg, genome, ncells=None, device=0, simulate_wo_barr
             t = prepare_chrom(eng, cfg, chrom, barriers, ncells)
             preps.append(t)
             bands[t["cid"]] = np.zeros(t["nrows"] * t["ncols"], dtype=np.uint32)
-            for seed, target in zip(t["seeds"], t["targets"]):
+            for seed, target in zip(t["seeds"][lo:hi], t["targets"][lo:hi]):
                 tasks.append((t["cid"], int(seed), int(target), t["target_epochs"], t["nlefs"]))
-        missed, stats = eng.simulate_batch(tasks, bands)
+        missed, stats = eng.simulate_batch(tasks, bands) if tasks else ({t["cid"]: 0 for t in preps}, [])
     out, k = [], 0
     for t in preps:
-        st = stats[k:k + ncells]
-        k += ncells
+        st = stats[k:k + hi - lo]
+        k += hi - lo
         out.append(ChromResult(t["chrom"], t["nlefs"], bands[t["cid"]], missed[t["cid"]], st))
     return out
 

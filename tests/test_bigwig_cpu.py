@@ -122,3 +122,71 @@ def test_occupancy_bigwig_file(tmp_path):
     vals = occupancy_values(occ)
     assert got == [(100_000 + k * 5000, 100_000 + (k + 1) * 5000, float(vals[k])) for k in range(nb)]
     assert d["intervals"]["chr2"] == []
+
+
+def test_file_layout_byte_by_byte(tmp_path):
+    """Decode a written file at the byte offsets of the published bigWig layout (Kent et al.,
+    Bioinformatics 26:2204, supplementary tables), without the module's reader or structs:
+    the 64-byte header, the 24-byte zoom headers, the 40-byte total summary, the chromosome
+    B+ tree (32-byte header, 4-byte node headers, key + id + size leaves), the 64-bit section
+    count at the data offset, the 24-byte section headers, and the R-tree index (48-byte
+    header whose end-of-data field equals the index offset, 32-byte leaf items)."""
+    import zlib
+
+    chroms = [("chrB", 40_000), ("chrA10", 90_001)]
+    tracks = [bw.Track("chrA10", 1, 1000, 1000, np.arange(90, dtype=np.float32)),
+              bw.Track("chrB", 0, 500, 500, np.full(80, 0.5, np.float32))]
+    p = tmp_path / "layout.bw"
+    bw.write_bigwig(str(p), chroms, tracks, items_per_slot=64)
+    buf = open(p, "rb").read()
+    u16 = lambda o: struct.unpack_from("<H", buf, o)[0]  # noqa: E731
+    u32 = lambda o: struct.unpack_from("<I", buf, o)[0]  # noqa: E731
+    u64 = lambda o: struct.unpack_from("<Q", buf, o)[0]  # noqa: E731
+    # header
+    assert u32(0) == 0x888FFC26 and u16(4) == 4
+    nz = u16(6)
+    tree_off, data_off, index_off = u64(8), u64(16), u64(24)
+    assert u16(32) == 0 and u16(34) == 0 and u64(36) == 0  # fieldCount, definedFieldCount, autoSql
+    summary_off, max_raw = u64(44), u32(52)
+    assert u64(56) == 0
+    assert summary_off == 64 + 24 * nz and tree_off == summary_off + 40 and nz >= 1
+    # total summary: bases covered, min, max, sum, sum of squares
+    covered, vmin, vmax, vsum, vsq = struct.unpack_from("<Qdddd", buf, summary_off)
+    assert covered == 90 * 1000 + 80 * 500 and vmin == 0.0 and vmax == 89.0
+    assert vsum == pytest.approx(1000 * sum(range(90)) + 500 * 0.5 * 80)
+    # chromosome B+ tree
+    assert u32(tree_off) == 0x78CA8C91
+    block, key_size, val_size, count = u32(tree_off + 4), u32(tree_off + 8), u32(tree_off + 12), u64(tree_off + 16)
+    assert key_size == len("chrA10") and val_size == 8 and count == 2 and block >= 2
+    node = tree_off + 32
+    assert buf[node] == 1 and u16(node + 2) == 2  # one leaf with both chromosomes
+    leaf = []
+    for k in range(2):
+        it = node + 4 + k * (key_size + 8)
+        leaf.append((buf[it:it + key_size].rstrip(b"\0").decode(), u32(it + key_size), u32(it + key_size + 4)))
+    assert leaf == [("chrA10", 0, 90_001), ("chrB", 1, 40_000)]  # byte order of the names
+    # data: a 64-bit section count, then zlib sections with 24-byte headers (type 3 = fixed step)
+    nsec = u64(data_off)
+    assert nsec == 2 + 2  # 90 values -> 2 sections of <= 64, 80 values -> 2
+    # R-tree index of the sections
+    assert u32(index_off) == 0x2468ACE0
+    assert u64(index_off + 8) == nsec and u64(index_off + 32) == index_off and u32(index_off + 40) == 64
+    node = index_off + 48
+    assert buf[node] == 1 and u16(node + 2) == nsec
+    seen = 0
+    for k in range(nsec):
+        it = node + 4 + 32 * k
+        sc, sb, ec, eb, off, size = struct.unpack_from("<IIIIQQ", buf, it)
+        raw = zlib.decompress(buf[off:off + size])
+        assert len(raw) <= max_raw
+        cid, s, e, step, span, typ, _, n = struct.unpack_from("<IIIIIBBH", raw, 0)
+        assert (cid, s, e) == (sc, sb, eb) and sc == ec and typ == 3 and len(raw) == 24 + 4 * n
+        seen += n
+        assert data_off + 8 <= off < index_off
+    assert seen == 170
+    # zoom headers: reduction level, reserved, data offset (32-bit record count), index offset
+    for z in range(nz):
+        red, res, zdata, zindex = struct.unpack_from("<IIQQ", buf, 64 + 24 * z)
+        assert res == 0 and zdata < zindex <= len(buf) - 48 and u32(zindex) == 0x2468ACE0
+        assert u64(zindex + 32) == zindex  # its data ends where its index starts
+        assert red == 1000 * 4 ** (z + 1)

@@ -235,3 +235,24 @@ def test_plan_windows_with_a_deletion_list(tmp_path):
     # generated deletions: one per barrier, ending one bp after it
     gen_plan = perturbate.plan_windows(cfg, gen, deletion_size=30_000)
     assert {c.name for c, _ in gen_plan} == {"chrD0", "chrD1"}
+
+
+def test_deletion_list_skipping_a_middle_chromosome_keeps_task_ids_contiguous(tmp_path):
+    """A deletion list that omits a chromosome between two listed ones and names one the genome
+    lacks (the reference looks deletions up per chromosome and skips chromosomes without any,
+    scheduler_perturbate.cpp:202): the omitted and the unknown chromosome give no task, and the
+    run-wide task ids run on without a gap from the first listed chromosome to the next."""
+    cfg = genome.parity_config(diagonal_width=500_000)
+    chroms = [engine.Chromosome(f"chrM{k}", 1_800_000) for k in range(3)]
+    rng = np.random.default_rng(8)
+    gen = [(ch, engine.barriers_from_bed(ch, genome.bed_records(rng, ch.size, 10), 0.7, 0.7)) for ch in chroms]
+    bed = tmp_path / "del.bed"
+    bed.write_text("chrM2\t300000\t330000\nchrUn\t5\t9\nchrM0\t700000\t720000\n")
+    dels = perturbate.read_bed_intervals(str(bed))
+    planned = perturbate.plan_windows(cfg, gen, deletions=dels)
+    names = [c.name for c, _ in planned]
+    assert set(names) == {"chrM0", "chrM2"} and "chrM1" not in names
+    assert names == sorted(names, key=lambda n: int(n[-1]))  # genome order: chrM0's tasks first
+    assert [t["task_id"] for _, t in planned] == list(range(len(planned)))
+    first_m2 = names.index("chrM2")
+    assert 0 < first_m2 and planned[first_m2][1]["task_id"] == planned[first_m2 - 1][1]["task_id"] + 1

@@ -185,3 +185,75 @@ def test_window_queue_over_two_gloo_ranks_equals_one_process():
     assert [t["task_id"] for _, t in sharding.shard_windows(planned, 2, 1)] == list(range(5, 10))
     want = perturbate.perturbate_records(cfg, feats1, feats2, ref, _oracle_windows(cfg, planned), block_size=3)
     assert want and got[0] == want and got[1] == want
+
+
+def _perturbate_case():
+    from modlefork_gb300 import engine, genome
+
+    cfg = genome.parity_config(diagonal_width=500_000)
+    rng = np.random.default_rng(12)
+    gen, feats1, feats2 = [], {}, {}
+    for k, L in enumerate((2_400_000, 1_800_000)):
+        ch = engine.Chromosome(f"chrQ{k}", L)
+        gen.append((ch, engine.barriers_from_bed(ch, genome.bed_records(rng, L, 30), 0.7, 0.7)))
+        for feats, tag in ((feats1, "a"), (feats2, "b")):
+            pos = np.sort(rng.integers(0, L - 1000, 25))
+            feats[ch.name] = [(ch.name, int(p), int(p) + 500, f"{tag}{i}", "+") for i, p in enumerate(pos)]
+    ref = {}
+    for ch, _ in gen:
+        nrows, ncols = engine.band_shape(cfg, ch.simulated_size)
+        ref[ch.name] = rng.integers(0, 5, nrows * ncols).astype(np.uint32)
+    return cfg, gen, feats1, feats2, ref
+
+
+def _perturbate_rank_main(rank, world, port, outdir):
+    import sys
+
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    import torch
+    import torch.distributed as dist
+
+    from modlefork_gb300 import perturbate
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        cfg, gen, feats1, feats2, ref = _perturbate_case()
+        lines, ntasks = perturbate.run(cfg, gen, feats1, feats2, deletion_size=60_000, block_size=3, max_tasks=10,
+                                       world=world, rank=rank, reference=lambda c, g: ref,
+                                       windows_fn=_oracle_windows)
+        if rank == 0:
+            perturbate.write_bedpe(os.path.join(outdir, "ranks.bedpe"), lines)
+        # the reference bands' exact sum over ranks: uint32 counts as int32, wrapping like uint32
+        band = np.array([1, 2**31 + 5, 2**32 - 1, 7], dtype=np.uint32) + np.uint32(rank)
+        t = torch.from_numpy(band.view(np.int32).copy())
+        from modlefork_gb300 import sharding
+
+        summed = sharding.allreduce_band_(t).numpy().view(np.uint32)
+        np.save(os.path.join(outdir, f"band{rank}.npy"), summed)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_perturbate_command_over_two_gloo_ranks_writes_the_single_rank_bedpe():
+    import torch.multiprocessing as mp
+
+    from modlefork_gb300 import perturbate
+
+    world = 2
+    with tempfile.TemporaryDirectory() as d:
+        mp.start_processes(_perturbate_rank_main, args=(world, _free_port(), d), nprocs=world,
+                           start_method="spawn", join=True)
+        got = open(os.path.join(d, "ranks.bedpe")).read()
+        bands = [np.load(os.path.join(d, f"band{r}.npy")) for r in range(world)]
+        cfg, gen, feats1, feats2, ref = _perturbate_case()
+        lines, ntasks = perturbate.run(cfg, gen, feats1, feats2, deletion_size=60_000, block_size=3, max_tasks=10,
+                                       reference=lambda c, g: ref, windows_fn=_oracle_windows)
+        perturbate.write_bedpe(os.path.join(d, "one.bedpe"), lines)
+        want = open(os.path.join(d, "one.bedpe")).read()
+    assert ntasks == 10 and len(lines) > 0 and got == want
+    base = np.array([1, 2**31 + 5, 2**32 - 1, 7], dtype=np.uint64)
+    expect = ((2 * base + 1) % 2**32).astype(np.uint32)
+    for b in bands:
+        assert np.array_equal(b, expect)

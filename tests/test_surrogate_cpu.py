@@ -84,3 +84,40 @@ def test_sweep_window_track_and_fp64_target():
     t = sweep.target_fp64(band.reshape(-1))
     assert np.allclose(t[5, :3], np.log1p(np.array([4, 2, 0]) * sweep.NROWS / 6.0))
     assert not t[6].any()
+
+
+def test_sweep_resumes_from_its_shards(tmp_path, monkeypatch):
+    """An interrupted sweep re-run with the same output directory simulates only the chunks
+    whose shard is missing, and load_shards returns every set in index order."""
+    from modlefork_gb300 import sweep
+
+    calls = []
+
+    class FakeTensor:
+        def __init__(self, a):
+            self.a = a
+
+        def cpu(self):
+            return self
+
+        def numpy(self):
+            return self.a
+
+    def fake(ks, seed, cells, density, device):
+        calls.append(list(ks))
+        n = len(ks)
+        return {"track": FakeTensor(np.full((n, 4, 3), ks[0], np.float32)),
+                "params": FakeTensor(np.asarray(ks, np.float32)[:, None].repeat(4, 1)),
+                "target": FakeTensor(np.zeros((n, 2, 2), np.float32)), "fp64_max_rel_dev": 0.0, "ms": 1.0,
+                "cells": n * cells, "lef_epochs": 0, "contacts": 0}
+
+    monkeypatch.setattr(sweep, "simulate_sets", fake)
+    out = str(tmp_path / "sweep")
+    sweep.generate(10, out_dir=out, chunk=4, cells=2)
+    assert calls == [[0, 1, 2, 3], [4, 5, 6, 7], [8, 9]]
+    os.remove(os.path.join(out, "shard_000004.npz"))  # the run that lost a chunk
+    calls.clear()
+    _, totals = sweep.generate(10, out_dir=out, chunk=4, cells=2)
+    assert calls == [[4, 5, 6, 7]] and totals["skipped"] == 6 and totals["maps"] == 4
+    ks, track, params, target = sweep.load_shards(out)
+    assert list(ks) == list(range(10)) and params[:, 0].tolist() == list(range(10))
