@@ -61,6 +61,12 @@ int msur_conv_forward(const void* x, int B, int L, int Cin, const void* w, int C
  * msur_conv_get_stages returns the current depth (negative on a bad width). */
 int msur_conv_set_stages(int bn, int stages);
 int msur_conv_get_stages(int bn);
+/* Kernel form of msur_conv_forward for one N tile width: 0 = one CTA per output tile; 1 = a
+ * persistent kernel (CTAs walk the tiles with a double-buffered TMEM accumulator, so a tile's
+ * epilogue overlaps the next tile's MMAs).  Results are identical; the default is 0 and the
+ * autotuner picks per device.  The getter returns the current form (negative on a bad width). */
+int msur_conv_set_persistent(int bn, int on);
+int msur_conv_get_persistent(int bn);
 
 /* Weight gradient of that convolution, ADDED to dw [Cout][taps][Cin] (FP32):
  *   dw[n][t][c] += sum_{b, l} dz[b, l, n] * x[b, l + t - (taps - 1) / 2, c]

@@ -71,6 +71,82 @@ __host__ __device__ constexpr uint32_t tmem_cols() {
   return BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : (BN <= 256 ? 256 : 512)));
 }
 
+// Epilogue of one 32-column chunk of one output row: bias, the gated SiLU derivative, and
+// the FP32 / pre-activation / post-activation stores (columns >= n_valid dropped).
+__device__ __forceinline__ void conv_epilogue_chunk(const ConvArgs& a, float (&v)[32], size_t row, int col0) {
+  const int nv = min(32, a.n_valid - col0);
+  const size_t off = row * a.out_stride + col0;
+  if (a.bias) {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] += (j < nv) ? __ldg(a.bias + col0 + j) : 0.0f;
+  }
+  if (a.gate) {
+    if (nv == 32) {
+      const uint4* g4 = reinterpret_cast<const uint4*>(a.gate + off);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const uint4 u = __ldg(g4 + k);
+        const uint32_t w4[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const __nv_bfloat162 g2 = *reinterpret_cast<const __nv_bfloat162*>(&w4[h]);
+          v[8 * k + 2 * h] *= dsilu(__low2float(g2));
+          v[8 * k + 2 * h + 1] *= dsilu(__high2float(g2));
+        }
+      }
+    } else {
+      for (int j = 0; j < nv; ++j) v[j] *= dsilu(__bfloat162float(a.gate[off + j]));
+    }
+  }
+  if (a.out_f32) {
+    if (nv == 32) {
+      float4* o4 = reinterpret_cast<float4*>(a.out_f32 + off);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) o4[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    } else {
+      for (int j = 0; j < nv; ++j) a.out_f32[off + j] = v[j];
+    }
+  }
+  if (a.out_pre) {
+    if (nv == 32) {
+      uint4* o4 = reinterpret_cast<uint4*>(a.out_pre + off);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        uint32_t w4[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const __nv_bfloat162 p = __floats2bfloat162_rn(v[8 * k + 2 * h], v[8 * k + 2 * h + 1]);
+          w4[h] = *reinterpret_cast<const uint32_t*>(&p);
+        }
+        o4[k] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+      }
+    } else {
+      for (int j = 0; j < nv; ++j) a.out_pre[off + j] = __float2bfloat16(v[j]);
+    }
+  }
+  if (a.out_post) {
+    if (a.act == MSUR_ACT_SILU) {
+#pragma unroll
+      for (int j = 0; j < 32; ++j) v[j] = silu(v[j]);
+    }
+    if (nv == 32) {
+      uint4* o4 = reinterpret_cast<uint4*>(a.out_post + off);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        uint32_t w4[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const __nv_bfloat162 p = __floats2bfloat162_rn(v[8 * k + 2 * h], v[8 * k + 2 * h + 1]);
+          w4[h] = *reinterpret_cast<const uint32_t*>(&p);
+        }
+        o4[k] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+      }
+    } else {
+      for (int j = 0; j < nv; ++j) a.out_post[off + j] = __float2bfloat16(v[j]);
+    }
+  }
+}
+
 template <int BN, int STAGES>
 __global__ void __launch_bounds__(THREADS, 1) conv_fwd_kernel(const __grid_constant__ ConvArgs a) {
   constexpr int A_BYTES = BM * BK * 2;
@@ -157,78 +233,146 @@ __global__ void __launch_bounds__(THREADS, 1) conv_fwd_kernel(const __grid_const
         umma::tmem_ld32(tmem + (static_cast<uint32_t>(32 * q) << 16) + c * 32, v);
         const int col0 = n0 + c * 32;
         if (!row_ok || col0 >= a.n_valid) continue;
-        const int nv = min(32, a.n_valid - col0);
-        const size_t off = row * a.out_stride + col0;
-        if (a.bias) {
-#pragma unroll
-          for (int j = 0; j < 32; ++j) v[j] += (j < nv) ? __ldg(a.bias + col0 + j) : 0.0f;
-        }
-        if (a.gate) {
-          if (nv == 32) {
-            const uint4* g4 = reinterpret_cast<const uint4*>(a.gate + off);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              const uint4 u = __ldg(g4 + k);
-              const uint32_t w4[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-              for (int h = 0; h < 4; ++h) {
-                const __nv_bfloat162 g2 = *reinterpret_cast<const __nv_bfloat162*>(&w4[h]);
-                v[8 * k + 2 * h] *= dsilu(__low2float(g2));
-                v[8 * k + 2 * h + 1] *= dsilu(__high2float(g2));
-              }
-            }
-          } else {
-            for (int j = 0; j < nv; ++j) v[j] *= dsilu(__bfloat162float(a.gate[off + j]));
+        conv_epilogue_chunk(a, v, row, col0);
+      }
+    }
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 1) {
+    umma::fence_after_sync();
+    umma::tmem_dealloc(tmem, TCOLS);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// The same convolution as a persistent kernel: each CTA walks tiles t = blockIdx.x,
+// blockIdx.x + gridDim.x, ... (N tile fastest, then position tile, then sequence) with a
+// double-buffered TMEM accumulator, so the epilogue of one tile overlaps the MMAs of the next
+// and a CTA's set-up (barriers, TMEM allocation, tensor-map prefetch) is paid once.
+// Barriers: full / empty per smem stage (TMA <-> MMA), tfull / tempty per accumulator
+// (MMA <-> the 128 epilogue threads), done (the MMA issuer's last commit).
+// ---------------------------------------------------------------------------------------
+template <int BN, int STAGES>
+__global__ void __launch_bounds__(THREADS, 1) conv_fwd_persistent_kernel(const __grid_constant__ ConvArgs a, int ntn,
+                                                                         int ntl, int ntiles) {
+  constexpr int A_BYTES = BM * BK * 2;
+  constexpr int B_BYTES = BN * BK * 2;
+  constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  constexpr uint32_t TCOLS = tmem_cols<2 * BN>();
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* tfull = empty + STAGES;
+  uint64_t* tempty = tfull + 2;
+  uint64_t* done = tempty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int kc = a.Cin / BK;
+  const int nk = a.taps * kc;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      umma::mbar_init(&full[s], 1);
+      umma::mbar_init(&empty[s], 1);
+    }
+    for (int k = 0; k < 2; ++k) {
+      umma::mbar_init(&tfull[k], 1);
+      umma::mbar_init(&tempty[k], 128);
+    }
+    umma::mbar_init(done, 1);
+    umma::fence_barrier_init();
+    umma::tma_prefetch(&a.tm_a);
+    umma::tma_prefetch(&a.tm_b);
+  }
+  if (warp == 1) umma::tmem_alloc(tmem_slot, TCOLS);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int s = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const int n0 = (t % ntn) * BN;
+        const int l0 = ((t / ntn) % ntl) * BM;
+        const int b = t / (ntn * ntl);
+        for (int kk = 0; kk < nk; ++kk, ++s) {
+          const int st = s % STAGES;
+          if (!umma::mbar_wait(&empty[st], ((s / STAGES) & 1) ^ 1, a.err, ERR_PRODUCER)) {
+            ok = false;
+            break;
           }
-        }
-        if (a.out_f32) {
-          if (nv == 32) {
-            float4* o4 = reinterpret_cast<float4*>(a.out_f32 + off);
-#pragma unroll
-            for (int k = 0; k < 8; ++k) o4[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
-          } else {
-            for (int j = 0; j < nv; ++j) a.out_f32[off + j] = v[j];
-          }
-        }
-        if (a.out_pre) {
-          if (nv == 32) {
-            uint4* o4 = reinterpret_cast<uint4*>(a.out_pre + off);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              uint32_t w4[4];
-#pragma unroll
-              for (int h = 0; h < 4; ++h) {
-                const __nv_bfloat162 p = __floats2bfloat162_rn(v[8 * k + 2 * h], v[8 * k + 2 * h + 1]);
-                w4[h] = *reinterpret_cast<const uint32_t*>(&p);
-              }
-              o4[k] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
-            }
-          } else {
-            for (int j = 0; j < nv; ++j) a.out_pre[off + j] = __float2bfloat16(v[j]);
-          }
-        }
-        if (a.out_post) {
-          if (a.act == MSUR_ACT_SILU) {
-#pragma unroll
-            for (int j = 0; j < 32; ++j) v[j] = silu(v[j]);
-          }
-          if (nv == 32) {
-            uint4* o4 = reinterpret_cast<uint4*>(a.out_post + off);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              uint32_t w4[4];
-#pragma unroll
-              for (int h = 0; h < 4; ++h) {
-                const __nv_bfloat162 p = __floats2bfloat162_rn(v[8 * k + 2 * h], v[8 * k + 2 * h + 1]);
-                w4[h] = *reinterpret_cast<const uint32_t*>(&p);
-              }
-              o4[k] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
-            }
-          } else {
-            for (int j = 0; j < nv; ++j) a.out_post[off + j] = __float2bfloat16(v[j]);
-          }
+          uint8_t* sa = smem + st * STAGE_BYTES;
+          umma::mbar_arrive_expect_tx(&full[st], STAGE_BYTES);
+          const int tap = kk / kc, c0 = (kk % kc) * BK;
+          umma::tma_load_3d(sa, &a.tm_a, &full[st], c0, l0 + tap - a.pad, b);
+          umma::tma_load_2d(sa + A_BYTES, &a.tm_b, &full[st], tap * a.Cin + c0, n0);
         }
       }
+      // drain: every issued copy has landed before the block can exit
+      for (int q = s > STAGES ? s - STAGES : 0; q < s; ++q)
+        umma::mbar_wait(&full[q % STAGES], (q / STAGES) & 1, a.err, ERR_PRODUCER);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = umma::idesc_bf16_f32(BM, BN, false, false);
+      int s = 0, j = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++j) {
+        const int acc = j & 1;
+        if (!umma::mbar_wait(&tempty[acc], ((j >> 1) & 1) ^ 1, a.err, ERR_MMA)) break;
+        umma::fence_after_sync();
+        const uint32_t d = tmem + acc * BN;
+        for (int kk = 0; kk < nk; ++kk, ++s) {
+          const int st = s % STAGES;
+          if (!umma::mbar_wait(&full[st], (s / STAGES) & 1, a.err, ERR_MMA)) {
+            ok = false;
+            break;
+          }
+          umma::fence_after_sync();
+          const uint32_t sa = umma::smem_u32(smem + st * STAGE_BYTES);
+          const uint32_t sb = sa + A_BYTES;
+#pragma unroll
+          for (int k4 = 0; k4 < BK / 16; ++k4) {
+            umma::mma_bf16(d, umma::sdesc_sw128(sa + k4 * 32, 16, 1024), umma::sdesc_sw128(sb + k4 * 32, 16, 1024),
+                           idesc, (kk | k4) != 0);
+          }
+          umma::mma_commit(&empty[st]);
+        }
+        if (ok) umma::mma_commit(&tfull[acc]);
+      }
+      // every MMA this thread issued has completed before TMEM is released
+      umma::mma_commit(done);
+      umma::mbar_wait(done, 0, a.err, ERR_MMA);
+    }
+  } else {
+    const int q = warp & 3;
+    int j = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++j) {
+      const int acc = j & 1;
+      const bool ok = umma::mbar_wait(&tfull[acc], (j >> 1) & 1, a.err, ERR_EPILOGUE);
+      umma::fence_after_sync();
+      if (!ok) break;
+      const int n0 = (t % ntn) * BN;
+      const int l = ((t / ntn) % ntl) * BM + 32 * q + lane;
+      const int b = t / (ntn * ntl);
+      const bool row_ok = l < a.L;
+      const size_t row = static_cast<size_t>(b) * a.L + (row_ok ? l : 0);
+#pragma unroll 1
+      for (int c = 0; c < BN / 32; ++c) {
+        float v[32];
+        umma::tmem_ld32(tmem + (static_cast<uint32_t>(32 * q) << 16) + acc * BN + c * 32, v);
+        const int col0 = n0 + c * 32;
+        if (!row_ok || col0 >= a.n_valid) continue;
+        conv_epilogue_chunk(a, v, row, col0);
+      }
+      umma::fence_before_sync();
+      umma::mbar_arrive(&tempty[acc]);
     }
   }
   umma::fence_before_sync();
@@ -686,6 +830,8 @@ unsigned* g_dev_err[64] = {};
 // pipeline stages of the forward/data-gradient convolution per N tile width (64, 128, 256):
 // fewer stages let more CTAs share an SM, so one tile's epilogue overlaps another's main loop
 int g_conv_stages[3] = {4, 3, 4};
+// 1: the persistent kernel (double-buffered TMEM accumulator) for that N tile width
+int g_conv_persistent[3] = {0, 0, 0};
 
 int fail(int code, const char* fmt, ...) {
   va_list ap;
@@ -753,6 +899,26 @@ int launch_conv(const ConvArgs& a, int ntiles_n, cudaStream_t st) {
   dim3 grid(ntiles_n, (a.L + BM - 1) / BM, a.B);
   kern<<<grid, THREADS, smem, st>>>(a);
   return cuda_ok(cudaGetLastError(), "conv_fwd_kernel launch");
+}
+
+template <int BN, int STAGES>
+int launch_conv_persistent(const ConvArgs& a, int ntn, cudaStream_t st) {
+  constexpr int smem = STAGES * (BM * BK * 2 + BN * BK * 2) + 1024 + 256;
+  constexpr int tcols = static_cast<int>(tmem_cols<2 * BN>());
+  auto kern = conv_fwd_persistent_kernel<BN, STAGES>;
+  int rc = cuda_ok(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem), "smem attribute");
+  if (rc) return rc;
+  int dev = 0, sms = 0, per_sm = 0;
+  rc = cuda_ok(cudaGetDevice(&dev), "cudaGetDevice");
+  if (!rc) rc = cuda_ok(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  if (!rc) rc = cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem), "occupancy");
+  if (rc) return rc;
+  per_sm = std::max(1, std::min(per_sm, 512 / tcols));  // each resident CTA holds its accumulators in TMEM
+  const int ntl = (a.L + BM - 1) / BM;
+  const int ntiles = ntn * ntl * a.B;
+  const int grid = std::min(ntiles, sms * per_sm);
+  kern<<<grid, THREADS, smem, st>>>(a, ntn, ntl, ntiles);
+  return cuda_ok(cudaGetLastError(), "conv_fwd_persistent_kernel launch");
 }
 
 template <int BN, int NT, int STAGES>
@@ -832,7 +998,23 @@ int msur_conv_forward(const void* x, int B, int L, int Cin, const void* w, int C
   a.err = err;
   const int ntn = (Cout + BN - 1) / BN;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const int stages = g_conv_stages[BN == 256 ? 2 : (BN == 128 ? 1 : 0)];
+  const int slot = BN == 256 ? 2 : (BN == 128 ? 1 : 0);
+  const int stages = g_conv_stages[slot];
+  if (g_conv_persistent[slot]) {
+    if (BN == 256) {
+      if (stages == 2) return launch_conv_persistent<256, 2>(a, ntn, st);
+      if (stages == 3) return launch_conv_persistent<256, 3>(a, ntn, st);
+      return launch_conv_persistent<256, 4>(a, ntn, st);
+    }
+    if (BN == 128) {
+      if (stages == 2) return launch_conv_persistent<128, 2>(a, ntn, st);
+      if (stages == 4) return launch_conv_persistent<128, 4>(a, ntn, st);
+      return launch_conv_persistent<128, 3>(a, ntn, st);
+    }
+    if (stages == 2) return launch_conv_persistent<64, 2>(a, ntn, st);
+    if (stages == 3) return launch_conv_persistent<64, 3>(a, ntn, st);
+    return launch_conv_persistent<64, 4>(a, ntn, st);
+  }
   if (BN == 256) {
     if (stages == 2) return launch_conv<256, 2>(a, ntn, st);
     if (stages == 3) return launch_conv<256, 3>(a, ntn, st);
@@ -854,6 +1036,18 @@ int msur_conv_set_stages(int bn, int stages) {
   std::lock_guard<std::mutex> lk(g_mu);
   g_conv_stages[bn == 256 ? 2 : (bn == 128 ? 1 : 0)] = stages;
   return MSUR_OK;
+}
+
+int msur_conv_set_persistent(int bn, int on) {
+  if (bn != 64 && bn != 128 && bn != 256) return fail(MSUR_ERR_INVALID_ARG, "msur_conv_set_persistent: bad N tile");
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_conv_persistent[bn == 256 ? 2 : (bn == 128 ? 1 : 0)] = on ? 1 : 0;
+  return MSUR_OK;
+}
+
+int msur_conv_get_persistent(int bn) {
+  if (bn != 64 && bn != 128 && bn != 256) return fail(MSUR_ERR_INVALID_ARG, "msur_conv_get_persistent: bad N tile");
+  return g_conv_persistent[bn == 256 ? 2 : (bn == 128 ? 1 : 0)];
 }
 
 int msur_conv_get_stages(int bn) {

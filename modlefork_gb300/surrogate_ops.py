@@ -48,6 +48,8 @@ def load(path=LIB_PATH):
         "msur_compact_rows": (i32, [vp, i32, u64, i32, vp, vp]),
         "msur_conv_set_stages": (i32, [i32, i32]),
         "msur_conv_get_stages": (i32, [i32]),
+        "msur_conv_set_persistent": (i32, [i32, i32]),
+        "msur_conv_get_persistent": (i32, [i32]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(lib, name)
@@ -195,3 +197,12 @@ def conv_set_stages(bn, stages):
 
 def conv_get_stages(bn):
     return load().msur_conv_get_stages(bn)
+
+
+def conv_set_persistent(bn, on):
+    """Persistent (1) or one-CTA-per-tile (0) convolution kernel for N tile bn (64, 128, 256)."""
+    _check(load().msur_conv_set_persistent(bn, 1 if on else 0), "msur_conv_set_persistent")
+
+
+def conv_get_persistent(bn):
+    return load().msur_conv_get_persistent(bn)

@@ -50,23 +50,36 @@ def test_launch_table_is_validated():
         eng.set_launch_table([])  # clears
 
 
-def test_conv_pipeline_depths_give_the_same_outputs():
-    rng = np.random.default_rng(9)
+@pytest.mark.parametrize("Cout,gated", [(64, False), (128, True), (256, False), (640, False), (384, True)])
+def test_conv_kernel_forms_and_depths_give_the_same_outputs(Cout, gated):
+    """The one-CTA-per-tile and the persistent kernel, at every pipeline depth, give bit-identical
+    results (each tile's MMAs run in the same order); the first form is checked against FP64 in
+    test_surrogate_kernels_gpu.py.  Shapes cover several tiles per CTA, ragged position tiles,
+    several sequences and the SiLU gate of the data gradient."""
+    rng = np.random.default_rng(Cout)
+    B, L, Cin = 3, 1000, 128
+    x = torch.from_numpy(rng.standard_normal((B, L, Cin)).astype(np.float32)).to("cuda", torch.bfloat16)
+    w = torch.from_numpy((rng.standard_normal((Cout, 3, Cin)) / 20).astype(np.float32)).to("cuda", torch.bfloat16)
+    bias = torch.from_numpy(rng.standard_normal(Cout).astype(np.float32)).to("cuda")
+    gate = (torch.from_numpy(rng.standard_normal((B, L, Cout)).astype(np.float32)).to("cuda", torch.bfloat16)
+            if gated else None)
+    bn = 64 if Cout <= 64 else (256 if Cout % 256 == 0 else 128)
+    saved = (ops.conv_get_stages(bn), ops.conv_get_persistent(bn))
     outs = {}
-    for Cout in (64, 128, 256):
-        x = torch.from_numpy(rng.standard_normal((2, 300, 128)).astype(np.float32)).to("cuda", torch.bfloat16)
-        w = torch.from_numpy((rng.standard_normal((Cout, 3, 128)) / 20).astype(np.float32)).to("cuda", torch.bfloat16)
-        bn = Cout if Cout < 256 else 256
-        saved = ops.conv_get_stages(bn)
-        try:
+    try:
+        for persistent in (0, 1):
             for stages in (2, 3, 4):
+                ops.conv_set_persistent(bn, persistent)
                 ops.conv_set_stages(bn, stages)
-                y = torch.empty(2, 300, Cout, dtype=torch.float32, device="cuda")
-                ops.conv_forward(x, w, out_f32=y)
-                outs[(Cout, stages)] = y.cpu().numpy()
-        finally:
-            ops.conv_set_stages(bn, saved)
-        for stages in (3, 4):
-            assert np.array_equal(outs[(Cout, stages)], outs[(Cout, 2)])  # same MMA order: bit-identical
+                y = torch.empty(B, L, Cout, dtype=torch.float32, device="cuda")
+                post = torch.empty(B, L, Cout, dtype=torch.bfloat16, device="cuda")
+                ops.conv_forward(x, w, bias=bias, act=ops.ACT_SILU, out_f32=y, out_post=post, gate=gate)
+                outs[(persistent, stages)] = (y.cpu().numpy(), post.float().cpu().numpy())
+    finally:
+        ops.conv_set_stages(bn, saved[0])
+        ops.conv_set_persistent(bn, saved[1])
     torch.cuda.synchronize()
     assert ops.take_error() == 0
+    want = outs[(0, 2)]
+    for k, (y, post) in outs.items():
+        assert np.array_equal(y, want[0]) and np.array_equal(post, want[1]), k

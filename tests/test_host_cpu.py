@@ -180,3 +180,6 @@ def test_launch_setting_layout_and_surrogate_library_exports():
         surrogate_ops.conv_set_stages(128, 5)
     for bn, default in ((64, 4), (128, 3), (256, 4)):
         assert surrogate_ops.conv_get_stages(bn) == default
+        assert surrogate_ops.conv_get_persistent(bn) == 0
+    with pytest.raises(surrogate_ops.SurrogateKernelError):
+        surrogate_ops.conv_set_persistent(32, 1)
