@@ -2,13 +2,13 @@
 
   python -m modlefork_gb300.autotune [--out FILE] [--quick]
 
-1. Batched simulator, per cell-size bucket (LEFs per cell): for a synthetic chromosome of the
-   genome workload's kind with a typical LEF count of the bucket (contact density 0.3, so that
-   the trial holds contact epochs as well as burn-in), one batched launch per candidate
-   (shared-memory budget per cell, shared-memory carveout, cap of resident cells per SM), timed
-   with CUDA events; the fastest in LEF-epochs/s becomes the bucket's entry of the table that
-   mgpu_set_launch_table installs, unless it beats the engine's default (16 KiB, 60 %) by less
-   than 5 %, the trials' spread, in which case the default stays.  The settings only move per-LEF arrays between
+1. Batched simulator, per cell-size bucket (LEFs per cell): the engine's own workloads of that
+   size (sweep windows; the genome workload's chromosomes grouped by LEF count, with their
+   burn-in and contacts), one batched launch per candidate (shared-memory budget per cell,
+   shared-memory carveout, cap of resident cells per SM), timed with CUDA events; the fastest in
+   LEF-epochs/s becomes the bucket's entry of the table that mgpu_set_launch_table installs,
+   unless it beats the engine's default (16 KiB, 60 %) by less than 5 %, the trials' spread, in
+   which case the default stays.  The settings only move per-LEF arrays between
    shared memory and global slots, so every candidate simulates the same cells.
 2. Surrogate convolutions: the kernel form (one CTA per tile, or persistent) and pipeline depth
    (2-4 stages) per N tile width of msur_conv_forward, by coordinate descent on the network's
@@ -34,7 +34,8 @@ DEFAULT_FILE = os.path.join(DATA, "tuning_gb300.json")
 BUCKETS = [(512, 16_000_000), (2048, 64_000_000), (4096, 160_000_000), (1 << 40, 250_000_000)]
 FULL = 1 << 30  # a budget above the device limit: as much shared memory per cell as a block may have
 DEFAULT = (16384, 60, 0)  # the engine's setting of large batches without a table
-CANDIDATES = [DEFAULT, (FULL, 0, 0)] + [(kib * 1024, co, 0) for kib in (12, 20, 24, 32) for co in (60, 80)]
+CANDIDATES = [DEFAULT, (FULL, 0, 0), (12288, 60, 0), (20480, 60, 0), (24576, 60, 0), (24576, 80, 0),
+              (32768, 80, 0)]
 QUICK_CANDIDATES = [DEFAULT, (FULL, 0, 0), (24576, 70, 0), (12288, 80, 0), (32768, 80, 0)]
 MARGIN = 1.05  # a candidate replaces the default only when it is this much faster
 
@@ -50,40 +51,60 @@ def device_key():
     return f"{p.name}|{p.multi_processor_count}"
 
 
-def tune_simulator(candidates, cells, density=0.3, device=0):
-    import torch
+def bucket_workloads():
+    """The workloads each bucket is tuned on, the engine's own: sweep windows for small cells, and
+    the genome workload's chromosomes grouped by LEF count (with their burn-in and contacts, as
+    the batched genome launch runs them).  Yields (max_lefs, description, [(cfg, chrom, barriers,
+    cells)])."""
+    from . import engine, genome, sweep
 
+    wins = [sweep.window(k, cells=1024, density=5.0) for k in range(12)]
+    yield 512, "sweep windows 0-11 (20 Mbp, 1024 cells, contact density 5)", [(w[0], w[1], w[2], 1024) for w in wins]
+    for lo, hi, cells in ((0, 2048, 1536), (2048, 4096, 1024), (4096, 1 << 40, 1024)):
+        cfg, gen = genome.genome_24chr(seed=11, num_cells=cells)  # per-cell targets split over `cells`
+        nl = {c.name: engine.num_lefs(cfg, c.simulated_size) for c, _ in gen}
+        chroms = [(cfg, c, b, cells) for c, b in gen if lo < nl[c.name] <= hi]
+        yield hi, (f"genome chromosomes with {lo + 1}-{min(hi, 99999)} LEFs ({len(chroms)}) x {cells} cells, "
+                   "contact density 1"), chroms
+
+
+def tune_simulator(candidates, device=0):
+    """One batched launch of each bucket's workload per candidate, timed with CUDA events."""
     from . import engine, genome
 
-    rng = np.random.default_rng(5)
     table, trials = [], []
-    for max_lefs, length in BUCKETS:
-        cfg = genome.genome_config(target_contact_density=density, num_cells=cells)
-        chrom = engine.Chromosome(f"tune{length // 1000000}", length)
-        nb = int(round(length / 50_000))
-        recs = genome.bed_records(rng, length, nb, rng.beta(8.0, 2.0, size=nb))
-        bars = engine.barriers_from_bed(chrom, recs, cfg.barrier_occupied_stp, cfg.barrier_not_occupied_stp)
-        nl = engine.num_lefs(cfg, chrom.simulated_size)
-        tg, te = engine.task_targets(cfg, chrom.simulated_size, nl, cells)
-        nrows, ncols = engine.band_shape(cfg, chrom.simulated_size)
-        band = torch.zeros(nrows * ncols, dtype=torch.int32, device=f"cuda:{device}")
+    for max_lefs, what, items in bucket_workloads():
         best, default_rate = None, 0.0
-        with engine.Engine(cfg, device) as eng:
-            cid = eng.upload_chrom(chrom, bars)
-            tasks = [(cid, engine.cell_seed(chrom.name, chrom.size, cfg.seed, i), int(tg[i]), te, nl)
-                     for i in range(cells)]
+        with engine.Engine(genome.genome_config(), device) as eng:
+            tasks, bands = [], {}
+            for cfg, chrom, bars, cells in items:
+                cid = eng.upload_chrom(chrom, bars)
+                eng.set_chrom_config(cid, cfg)
+                n = engine.num_lefs(cfg, chrom.simulated_size)
+                tg, te = engine.task_targets(cfg, chrom.simulated_size, n, cells)
+                bands[cid] = None
+                tasks += [(cid, engine.cell_seed(chrom.name, chrom.size, cfg.seed, i), int(tg[i]), te, n)
+                          for i in range(cells)]
+            import torch
+
+            dbands = {}
+            for (cfg, chrom, _, _), cid in zip(items, sorted(bands)):
+                dbands[cid] = torch.zeros(int(np.prod(engine.band_shape(cfg, chrom.simulated_size))),
+                                          dtype=torch.int32, device=f"cuda:{device}")
+            ptrs = {c: t.data_ptr() for c, t in dbands.items()}
+            log(f"bucket <= {max_lefs} LEFs: {what}, {len(tasks)} cells")
             for budget, carveout, cap in candidates:
                 eng.set_debug_flags(((carveout & 0xFF) << 8) | ((cap & 0xFF) << 16), budget)
                 try:
-                    _, st = eng.simulate_batch(tasks, {cid: band.data_ptr()})
-                except engine.EngineError as e:  # a budget below the cell's fixed shared memory
-                    log(f"{nl} LEFs: budget {budget // 1024} KiB rejected ({e})")
+                    _, st = eng.simulate_batch(tasks, ptrs)
+                except engine.EngineError as e:  # a budget below a cell's fixed shared memory
+                    log(f"  budget {budget // 1024} KiB rejected ({e})")
                     continue
                 ms = eng.last_kernel_ms()
-                rate = sum(s.lef_epochs for s in st) / (ms / 1e3)
-                trials.append({"bucket_max_lefs": max_lefs, "lefs": nl, "smem_budget": budget,
+                rate = sum(x.lef_epochs for x in st) / (ms / 1e3)
+                trials.append({"bucket_max_lefs": max_lefs, "workload": what, "smem_budget": budget,
                                "carveout_pct": carveout, "max_cells_per_sm": cap, "ms": ms, "lef_epochs_per_s": rate})
-                log(f"{nl} LEFs: budget {min(budget, 1 << 20) // 1024} KiB, carveout {carveout} %, cap {cap}: "
+                log(f"  budget {min(budget, 1 << 20) // 1024} KiB, carveout {carveout} %, cap {cap}: "
                     f"{rate:.3e} LEF-epochs/s")
                 if (budget, carveout, cap) == DEFAULT:
                     default_rate = rate
@@ -92,8 +113,8 @@ def tune_simulator(candidates, cells, density=0.3, device=0):
         if best[0] < MARGIN * default_rate:  # within the measurement's spread: keep the default
             best = (default_rate,) + DEFAULT
         table.append({"max_lefs": max_lefs, "smem_budget": best[1], "carveout_pct": best[2],
-                      "max_cells_per_sm": best[3], "lef_epochs_per_s": best[0], "default_lef_epochs_per_s": default_rate,
-                      "trial_lefs": nl})
+                      "max_cells_per_sm": best[3], "lef_epochs_per_s": best[0],
+                      "default_lef_epochs_per_s": default_rate, "workload": what})
     return table, trials
 
 
@@ -186,7 +207,6 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--out", default="tuning.json")
     ap.add_argument("--quick", action="store_true", help="five simulator candidates instead of nineteen")
-    ap.add_argument("--cells", type=int, default=1600)
     ap.add_argument("--only", choices=["simulator", "surrogate"], default=None,
                     help="tune one part and keep the other's entry from --out")
     args = ap.parse_args(argv)
@@ -200,7 +220,7 @@ def main(argv=None):
     entry.setdefault("trials", {})
     if args.only != "surrogate":
         cands = QUICK_CANDIDATES if args.quick else CANDIDATES
-        entry["simulator"], entry["trials"]["simulator"] = tune_simulator(cands, args.cells)
+        entry["simulator"], entry["trials"]["simulator"] = tune_simulator(cands)
     if args.only != "simulator":
         entry["surrogate"], entry["trials"]["surrogate"] = tune_surrogate()
     entry["measured"] = time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())
