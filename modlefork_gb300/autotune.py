@@ -11,8 +11,8 @@
    which case the default stays.  The settings only move per-LEF arrays between
    shared memory and global slots, so every candidate simulates the same cells.
 2. Surrogate convolutions: the kernel form (one CTA per tile, or persistent) and pipeline depth
-   (2-4 stages) per N tile width of msur_conv_forward, by coordinate descent on the network's
-   inference time at batch 256.
+   (2-4 stages) per N tile width of msur_conv_forward, then per forward layer of the network,
+   by coordinate descent on the network's inference time at batch 256.
 
 The result is a JSON file keyed by the device's name and SM count; ``load_table`` and
 ``apply_all`` read it back (engine contexts and the surrogate library take it from there).  The
@@ -124,6 +124,7 @@ def tune_surrogate(batch=256, reps=5):
     from . import surrogate as S
     from . import surrogate_ops as ops
 
+    S.LAYER_CFG.clear()  # start from the per-width settings alone
     net = S.UNet(seed=0)
     x = torch.zeros(batch, net.length, S.IN_CH, dtype=torch.bfloat16, device=net.dev)
     x[:, :, :8].normal_()
@@ -157,10 +158,32 @@ def tune_surrogate(batch=256, reps=5):
             ops.conv_set_persistent(bn, choice[bn][0])
             ops.conv_set_stages(bn, choice[bn][1])
             log(f"conv N tile {bn}: {times} -> {choice[bn]}")
+    per_width = timed()
+    # then per forward layer (the network sets the layer's choice before its call), starting
+    # from the per-width choices, one round of coordinate descent over the layers
+    layers = {}
+    for name, spec in net.specs.items():
+        layers[name] = choice[S.tile_width(spec.cout)]
+    S.LAYER_CFG.clear()
+    S.LAYER_CFG.update(layers)
+    cur = timed()
+    for name in net.specs:
+        times = {}
+        for persistent in (0, 1):
+            for stages in (2, 3, 4):
+                S.LAYER_CFG[name] = (persistent, stages)
+                times[(persistent, stages)] = timed()
+        best_cfg = min(times, key=times.get)
+        S.LAYER_CFG[name] = best_cfg
+        trials.append({"layer": name, "times": {f"{k[0]},{k[1]}": v for k, v in times.items()}})
+        log(f"layer {name}: -> {best_cfg} ({times[best_cfg]:.3f} ms)")
     best = timed()
-    return {"stages": {str(k): v[1] for k, v in choice.items()},
-            "persistent": {str(k): v[0] for k, v in choice.items()}, "ms_per_batch_default": base,
-            "ms_per_batch_tuned": best, "batch": batch}, trials
+    out = {"stages": {str(k): v[1] for k, v in choice.items()},
+           "persistent": {str(k): v[0] for k, v in choice.items()},
+           "layers": {k: list(v) for k, v in S.LAYER_CFG.items()}, "ms_per_batch_default": base,
+           "ms_per_batch_per_width": per_width, "ms_per_batch_tuned": best, "batch": batch}
+    S.LAYER_CFG.clear()
+    return out, trials
 
 
 def load_table(path=DEFAULT_FILE):
@@ -201,6 +224,10 @@ def apply_surrogate(tuned):
             ops.conv_set_stages(int(bn), int(stages))
         for bn, on in tuned["surrogate"].get("persistent", {}).items():
             ops.conv_set_persistent(int(bn), int(on))
+        from . import surrogate as S
+
+        S.LAYER_CFG.clear()
+        S.LAYER_CFG.update({k: (int(v[0]), int(v[1])) for k, v in tuned["surrogate"].get("layers", {}).items()})
 
 
 def main(argv=None):
