@@ -98,7 +98,7 @@ enum : u32 {
   PF_LEF_BAR, PF_PRIMARY, PF_CORRECT, PF_SECONDARY, PF_FIX, PF_EXTRUDE_RELEASE, PF_TRACE, PF_TOTAL,
   PF_RANK_FALLBACK, PF_ADJUST_FALLBACK, PF_CHAIN_SERIAL, PF_CONTACT_SERIAL, PF_FIX_FALLBACK,
   PF_REFILLS, PF_STALE_REFILLS, PF_EPOCHS, PF_RANK_PDQ, PF_RANK_PASS, PF_RANK_BLOCK, PF_RANK_MERGE,
-  PF_COUNT = 32
+  PF_RANK_SERIAL, PF_COUNT = 32
 };
 
 struct Scalars {
@@ -192,7 +192,7 @@ __device__ __forceinline__ void rng_ensure(Cell& c, u64* s, u32 n) {
 __device__ __forceinline__ u64 ring_at(const Cell& c, u64 k) { return c.ring[k & (RING - 1)]; }
 
 // Lane 0 only: next draw of the stream, generated serially when the ring is dry.
-__device__ u64 rng_serial(Cell& c) {
+__device__ __noinline__ u64 rng_serial(Cell& c) {
   Scalars* sc = c.sc;
   if (sc->rpos == sc->gpos) {
     const u64 v = xo_next(sc->canon);
@@ -394,14 +394,14 @@ __device__ int unit_normal_t(Src& g, double& out) {
   return SMP_LIMIT;
 }
 
-__device__ double s_unit_exponential(Cell& c) {
+__device__ __noinline__ double s_unit_exponential(Cell& c) {
   SerialSrc g{c, 0};
   double v = 0.0;
   if (unit_exponential_t(g, v) != SMP_OK) set_status(c, DEV_ERR_ITER_LIMIT);
   return v;
 }
 
-__device__ double s_unit_normal(Cell& c) {
+__device__ __noinline__ double s_unit_normal(Cell& c) {
   SerialSrc g{c, 0};
   double v = 0.0;
   if (unit_normal_t(g, v) != SMP_OK) set_status(c, DEV_ERR_ITER_LIMIT);
@@ -419,7 +419,7 @@ __device__ const double kLogFactorial[10] = {0.0,
                                              10.604602902745251,
                                              12.801827480081469};
 
-__device__ u64 s_poisson(Cell& c, const KParams& P) {
+__device__ __noinline__ u64 s_poisson(Cell& c, const KParams& P) {
   const double mean = P.pois_mean;
   if (mean < 10) {
     double p = P.pois_exp_mean;
@@ -482,7 +482,7 @@ __device__ double binomial_fc(i64 k) {
   return (1.0 / 12 - (1.0 / 360 - (1.0 / 1260) * (ikp1 * ikp1)) * (ikp1 * ikp1)) * ikp1;
 }
 
-__device__ i64 s_binomial(Cell& c, const KParams& P, i64 t_, double p_) {
+__device__ __noinline__ i64 s_binomial(Cell& c, const KParams& P, i64 t_, double p_) {
   const double p = (0.5 < p_) ? (1 - p_) : p_;
   const i64 t = t_;
   const i64 m = (i64)((t + 1) * p);
@@ -580,7 +580,7 @@ __device__ i64 s_binomial(Cell& c, const KParams& P, i64 t_, double p_) {
   return (0.5 < p_) ? t_ - res : res;
 }
 
-__device__ double s_gev(Cell& c, const KParams& P) {
+__device__ __noinline__ double s_gev(Cell& c, const KParams& P) {
   const double u = canonical_of(rng_serial(c));
   if (P.gev_xi == 0.0) return (P.gev_mu - P.gev_sigma) * log(-log(u));
   return P.gev_mu + (P.gev_sigma * (1.0 - pow(-log(u), P.gev_xi))) / P.gev_xi;
@@ -588,13 +588,15 @@ __device__ double s_gev(Cell& c, const KParams& P) {
 
 
 // ---------------------------------------------------------------------------------------
-// Serial restatements (lane 0): the exact fallbacks of the warp-parallel steps
+// Serial restatements (lane 0): the exact fallbacks of the warp-parallel steps.  They and the
+// serial samplers are kept out of line: the epoch loop's code is large enough that, with eight
+// or more cells per SM, instruction fetch stalls grow with its size.
 // ---------------------------------------------------------------------------------------
 
 // rank_lefs for one direction (simulation.cpp:402-487): split_sort (or pdq_sort at epoch 0)
 // by position, then runs of equal positions insertion-sorted by binding epoch (ascending
 // for rev units, descending for fwd units).
-__device__ void rank_dir_serial(Cell& c, u32 dir, u32 n, bool partially_sorted) {
+__device__ __noinline__ void rank_dir_serial(Cell& c, u32 dir, u32 n, bool partially_sorted) {
   u32* R = dir ? c.fr : c.rr;
   const u32* pos = dir ? c.fwd : c.rev;
   const KeyCmp cmp{pos};
@@ -619,7 +621,7 @@ __device__ void rank_dir_serial(Cell& c, u32 dir, u32 n, bool partially_sorted) 
 }
 
 // adjust_moves_of_consecutive_extr_units (simulation.cpp:343-399), one direction; lane 0
-__device__ void adjust_dir_serial(Cell& c, const KParams& P, u32 dir, u32 n) {
+__device__ __noinline__ void adjust_dir_serial(Cell& c, const KParams& P, u32 dir, u32 n) {
   if (n == 0) return;
   const u64 start = P.start, end = P.end;
   if (dir == 0) {
@@ -721,7 +723,7 @@ __device__ void detect_boundaries_serial(Cell& c, const KParams& P, u32 n, u64& 
 __device__ __forceinline__ bool bar_active(const Cell& c, u32 i) { return (c.bst[i >> 5] >> (i & 31)) & 1u; }
 
 // detect_lef_bar_collisions (simulation_detect_collisions.cpp:128-252); lane 0
-__device__ void detect_lef_bar_serial(Cell& c, const KParams& P, u32 n, u64 n5, u64 n3) {
+__device__ __noinline__ void detect_lef_bar_serial(Cell& c, const KParams& P, u32 n, u64 n5, u64 n3) {
   u64 j = min(n5, n5 - 1);
   u32 unit_idx = c.rr[j];
   u64 unit_pos = pos64(c.rev[unit_idx]);
@@ -802,7 +804,7 @@ __device__ __forceinline__ void primary_pair_update(Cell& c, u32 rev_idx, u32 fw
 }
 
 // detect_primary_lef_lef_collisions (simulation_detect_collisions.cpp:255-401); lane 0
-__device__ void detect_primary_serial(Cell& c, const KParams& P, u32 n, u64 n5, u64 n3) {
+__device__ __noinline__ void detect_primary_serial(Cell& c, const KParams& P, u32 n, u64 n5, u64 n3) {
   if (n5 == n || n3 == n) return;
   u64 i1 = 0, j1 = n5;
   const u64 i2 = n - min(n3, n3 - 1);
@@ -834,7 +836,7 @@ __device__ void detect_primary_serial(Cell& c, const KParams& P, u32 n, u64 n5, 
 }
 
 // process_secondary_lef_lef_collisions (simulation_detect_collisions.cpp:404-518); lane 0
-__device__ void process_secondary_serial(Cell& c, const KParams& P, u32 n, u64 n5, u64 n3) {
+__device__ __noinline__ void process_secondary_serial(Cell& c, const KParams& P, u32 n, u64 n5, u64 n3) {
   for (u64 i = max((u64)1, n5); i < n; ++i) {
     const u32 idx1 = c.rr[i - 1];
     if (!cw_occurred(c.rc[idx1])) continue;
@@ -919,7 +921,7 @@ __device__ __forceinline__ void fix_fwd_at(Cell& c, u64 end, u64 i) {
 }
 
 // fix_secondary_lef_lef_collisions (simulation_detect_collisions.cpp:520-647); lane 0
-__device__ void fix_secondary_serial(Cell& c, const KParams& P, u32 n, u64 n5, u64 n3) {
+__device__ __noinline__ void fix_secondary_serial(Cell& c, const KParams& P, u32 n, u64 n5, u64 n3) {
   const u64 num_active_fwd = n - min(n3, n3 - 1);
   for (u64 i = max((u64)1, n5); i < n; ++i) {
     if (cw_avoided_as(c.rc[c.rr[i]], EV_SECONDARY)) fix_rev_at(c, P.start, i);
@@ -1052,31 +1054,39 @@ __device__ __forceinline__ u64 rank_key(const Cell& c, u32 dir, u32 idx) {
   return ((u64)p << 32) | e;
 }
 
-// Warp bitonic sort of a[0..m) by ranking key.  Only ascending comparators are used (each merge
+// Warp bitonic sort of the index block a[0..m) by the 64-bit keys hi[k] << 32 | lo[k] stored
+// beside it (a, hi and lo move together).  Only ascending comparators are used (each merge
 // starts by comparing mirror pairs), so the virtual +inf padding up to a power of two never
-// moves and needs no storage.
-__device__ void bitonic_by_key(const Cell& c, u32 dir, u32* a, u32 m) {
-  u32 p2 = 1;
-  while (p2 < m) p2 <<= 1;
+// moves and needs no storage.  Block sizes and strides are powers of two, so the comparator
+// indexes are shifts and masks.
+__device__ void bitonic_keyed(u32* a, u32* hi, u32* lo, u32 m) {
+  u32 lg = 0;
+  while ((1u << lg) < m) ++lg;
+  const u32 ncmp = (1u << lg) >> 1;  // comparators per stage
   auto cmpx = [&](u32 i, u32 j) {
     if (j >= m) return;
-    const u32 x = a[i], y = a[j];
-    if (rank_key(c, dir, x) > rank_key(c, dir, y)) {
-      a[i] = y;
+    const u64 ki = ((u64)hi[i] << 32) | lo[i], kj = ((u64)hi[j] << 32) | lo[j];
+    if (ki > kj) {
+      hi[i] = (u32)(kj >> 32);
+      lo[i] = (u32)kj;
+      hi[j] = (u32)(ki >> 32);
+      lo[j] = (u32)ki;
+      const u32 x = a[i];
+      a[i] = a[j];
       a[j] = x;
     }
   };
-  for (u32 size = 2; size <= p2; size <<= 1) {
-    const u32 half = size >> 1;
-    for (u32 t = ln(); t < p2 / 2; t += 32) {
-      const u32 base = (t / half) * size, off = t % half;
-      cmpx(base + off, base + size - 1 - off);
+  for (u32 s = 1; s <= lg; ++s) {
+    // merge into sorted blocks of 2^s: mirror pairs, then strides 2^(s-2) .. 1
+    for (u32 t = ln(); t < ncmp; t += 32) {
+      const u32 base = (t >> (s - 1)) << s, off = t & ((1u << (s - 1)) - 1u);
+      cmpx(base + off, base + (1u << s) - 1u - off);
     }
     __syncwarp();
-    for (u32 stride = half >> 1; stride > 0; stride >>= 1) {
-      for (u32 t = ln(); t < p2 / 2; t += 32) {
-        const u32 i = 2 * stride * (t / stride) + (t % stride);
-        cmpx(i, i + stride);
+    for (int q = (int)s - 2; q >= 0; --q) {
+      for (u32 t = ln(); t < ncmp; t += 32) {
+        const u32 i = ((t >> q) << (q + 1)) | (t & ((1u << q) - 1u));
+        cmpx(i, i + (1u << q));
       }
       __syncwarp();
     }
@@ -1086,7 +1096,7 @@ __device__ void bitonic_by_key(const Cell& c, u32 dir, u32* a, u32 m) {
 // Lane 0: insertion-sort the run of equal positions around a[t-1], a[t] by binding epoch
 // (ascending for rev units, descending for fwd units), as the tie fix of rank_lefs does
 // (simulation.cpp:446-485).  Returns the end of the run.
-__device__ u32 tie_fix_run(const Cell& c, u32 dir, u32* a, u32 t, u32 len) {
+__device__ __noinline__ u32 tie_fix_run(const Cell& c, u32 dir, u32* a, u32 t, u32 len) {
   const u32* pos = dir ? c.fwd : c.rev;
   const u32 p = pos[a[t]];
   u32 lo = t - 1, hi = t + 1;
@@ -1115,16 +1125,21 @@ __device__ u32 tie_fix_run(const Cell& c, u32 dir, u32* a, u32 t, u32 len) {
 // removed block only changes by events (top prepended, reader appended) and by pushes (each
 // rotates it left by one), so every removed element's final slot follows from the event list.
 // B is sorted by key with a warp bitonic sort; only if B holds full ties is it pdq-sorted
-// exactly on lane 0.  Returns false (R untouched) when the event list does not fit.
+// exactly on lane 0.  Returns false (R untouched) for n < 2 or n > 65535.
+//
+// Scratch: the stack K in sr, the input positions and later B in tmp, and the event lists in
+// rm, fm and sf.  The move arrays are dead from binding until the moves are generated (the
+// callers that keep them restore them), and every event removes one input element, so n
+// entries per list always suffice.
 __device__ bool rank_dir_split(Cell& c, u32 dir, u32 n) {
   if (n < 2 || n > 0xFFFFu) return false;
   u32* R = dir ? c.fr : c.rr;
   const u32* pos = dir ? c.fwd : c.rev;
   u32* K = c.sr;
-  const u32 EMAX = n / 3;
-  u32* ev_q = c.sf;  // pushes since the previous event; later (q mod k_prev) | k_prev << 16
-  u32* ev_top = c.sf + EMAX;
-  u32* ev_rd = c.sf + 2 * EMAX;
+  const u32 EMAX = n;
+  u32* ev_q = c.rm;  // pushes since the previous event; later (q mod k_prev) | k_prev << 16
+  u32* ev_top = c.fm;
+  u32* ev_rd = c.sf;
   u32* B = c.tmp;
   const u32 lane = ln();
   u64 tprof = clock64();
@@ -1235,55 +1250,24 @@ __device__ bool rank_dir_split(Cell& c, u32 dir, u32 n) {
     }
   }
   __syncwarp();
-  // sort B by key (events are dead: sf is free).  When sf has room, the keys are loaded once
-  // and sorted alongside the indices, so the network compares values already in memory.
+  // sort B by key (the events are dead: sf, rm and fm are free); the keys are loaded once and
+  // sorted alongside the indices, so the network compares values already in memory.  Measured
+  // on the genome workload, sorting every block this way beats handing large blocks (or, as
+  // split_sort's event list once had to, whole ranks) to lane 0's serial sorts.
   u32* Bs = c.sf;
+  u32* Kh = c.rm;  // position
+  u32* Kl = c.fm;  // binding epoch (complemented for fwd units)
   bool full_tie = false;
-  if (3 * kE + 1 <= n) {
-    // 8-byte aligned start at or after sf + kE (sf itself is only 4-byte aligned when n is odd)
-    const u32 koff = kE + (u32)(((reinterpret_cast<uintptr_t>(c.sf) >> 2) + kE) & 1u);
-    u64* Kb = reinterpret_cast<u64*>(c.sf + koff);
-    for (u32 t = lane; t < kE; t += 32) {
-      const u32 idx = B[t];
-      Bs[t] = idx;
-      Kb[t] = rank_key(c, dir, idx);
-    }
-    __syncwarp();
-    u32 p2 = 1;
-    while (p2 < kE) p2 <<= 1;
-    auto cmpx = [&](u32 i, u32 j) {
-      if (j >= kE) return;
-      const u64 ki = Kb[i], kj = Kb[j];
-      if (ki > kj) {
-        Kb[i] = kj;
-        Kb[j] = ki;
-        const u32 x = Bs[i];
-        Bs[i] = Bs[j];
-        Bs[j] = x;
-      }
-    };
-    for (u32 size = 2; size <= p2; size <<= 1) {
-      const u32 half = size >> 1;
-      for (u32 t = lane; t < p2 / 2; t += 32) {
-        const u32 base = (t / half) * size, off = t % half;
-        cmpx(base + off, base + size - 1 - off);
-      }
-      __syncwarp();
-      for (u32 stride = half >> 1; stride > 0; stride >>= 1) {
-        for (u32 t = lane; t < p2 / 2; t += 32) {
-          const u32 i = 2 * stride * (t / stride) + (t % stride);
-          cmpx(i, i + stride);
-        }
-        __syncwarp();
-      }
-    }
-    for (u32 t = lane + 1; t < kE; t += 32) full_tie |= Kb[t - 1] == Kb[t];
-  } else {
-    for (u32 t = lane; t < kE; t += 32) Bs[t] = B[t];
-    __syncwarp();
-    bitonic_by_key(c, dir, Bs, kE);
-    for (u32 t = lane + 1; t < kE; t += 32) full_tie |= rank_key(c, dir, Bs[t - 1]) == rank_key(c, dir, Bs[t]);
+  for (u32 t = lane; t < kE; t += 32) {
+    const u32 idx = B[t];
+    const u64 k = rank_key(c, dir, idx);
+    Bs[t] = idx;
+    Kh[t] = (u32)(k >> 32);
+    Kl[t] = (u32)k;
   }
+  __syncwarp();
+  bitonic_keyed(Bs, Kh, Kl, kE);
+  for (u32 t = lane + 1; t < kE; t += 32) full_tie |= Kh[t - 1] == Kh[t] && Kl[t - 1] == Kl[t];
   const u32* Bf = Bs;
   if (__any_sync(FULL, full_tie)) {
     prof_add(c, PF_RANK_PDQ, 1);
@@ -1364,12 +1348,14 @@ __device__ void rank_lefs(Cell& c, const KParams& P, u32 n, u32 epoch, bool part
   for (u32 dir = 0; dir < 2; ++dir) {
     const bool ok = partially_sorted && !(P.debug_flags & DBG_SERIAL_RANK) && rank_dir_split(c, dir, n);
     if (!ok) {
+      const u64 t0 = clock64();
       prof_add(c, PF_RANK_FALLBACK, 1);
       if (ln() == 0) {
         rank_dir_serial(c, dir, n, partially_sorted);
         c.sc->sort_fallbacks++;
       }
       __syncwarp();
+      prof_add(c, PF_RANK_SERIAL, clock64() - t0);
     }
   }
 }
@@ -2469,7 +2455,7 @@ __device__ __forceinline__ void occ_increment(const KParams& P, u64 i1, u64 i2) 
 
 // One attempt of register_contacts_loop / _tad (register_contacts.cpp:129-198) or, with occ, of
 // register_1d_lef_occupancy (the loop attempt with the 1D counters as its sink); lane 0.
-__device__ void contact_attempt_serial(Cell& c, const KParams& P, bool tad, u64 na, bool* ok, bool* miss,
+__device__ __noinline__ void contact_attempt_serial(Cell& c, const KParams& P, bool tad, u64 na, bool* ok, bool* miss,
                                        bool occ = false) {
   *ok = false;
   *miss = false;
@@ -2598,7 +2584,7 @@ __device__ void sample_contacts(Cell& c, u64* s, const KParams& P, u64 target) {
 
 // sample_and_register_contacts with serial draws (lane 0): the exact path behind the
 // DBG_SERIAL_CONTACTS switch.
-__device__ void sample_contacts_serial(Cell& c, const KParams& P, u64 target) {
+__device__ __noinline__ void sample_contacts_serial(Cell& c, const KParams& P, u64 target) {
   Scalars* sc = c.sc;
   u64 num = P.spe;
   if (P.density_positive) num = min(num, target - sc->num_contacts);
@@ -2642,7 +2628,7 @@ __device__ __forceinline__ u64 mix64(u64 z) {
 }
 
 // mgpu_state_digest of the cell's state, and the full arrays when requested.
-__device__ void trace_record(Cell& c, const KParams& P, const DevTrace& T, u64 rec) {
+__device__ __noinline__ void trace_record(Cell& c, const KParams& P, const DevTrace& T, u64 rec) {
   const u32 nl = P.nlefs;
   const bool full = rec < T.max_records;
   u64 part = 0;
@@ -2761,7 +2747,7 @@ __device__ void cell_reset(Cell& c, u32 nl, u64 seed) {
 
 // Simulation::dump_stats (simulation.cpp:1166-1224): the epoch's model-state record, taken after
 // extrude and before release_lefs; the loop-size mean is exact (an integer sum below 2^53).
-__device__ void log_model_state(Cell& c, const KParams& P, u32 n, u64 cell) {
+__device__ __noinline__ void log_model_state(Cell& c, const KParams& P, u32 n, u64 cell) {
   Scalars* sc = c.sc;
   if (!P.records || sc->nrec >= P.rec_max) return;
   u32 st_rev = 0, st_fwd = 0, st_both = 0, lb = 0, pri = 0, sec = 0;
@@ -3113,14 +3099,18 @@ __global__ void __launch_bounds__(32) phase_kernel(const __grid_constant__ KPara
       break;
   }
   __syncwarp();
+  // rank_lefs uses the move arrays as scratch: the caller's moves stay as they were
+  const bool moves_kept = phase == MGPU_PHASE_BIND || phase == MGPU_PHASE_RANK;
   for (u32 i = ln(); i < n; i += 32) {
     A[0][i] = pos64(c.rev[i]);
     A[1][i] = pos64(c.fwd[i]);
     A[2][i] = pos64(c.bep[i]);
     A[3][i] = c.rr[i];
     A[4][i] = c.fr[i];
-    A[5][i] = c.rm[i];
-    A[6][i] = c.fm[i];
+    if (!moves_kept) {
+      A[5][i] = c.rm[i];
+      A[6][i] = c.fm[i];
+    }
     A[7][i] = cw_to_ref(c.rc[i]);
     A[8][i] = cw_to_ref(c.fc[i]);
   }

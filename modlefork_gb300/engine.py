@@ -442,7 +442,7 @@ class Engine:
                      "extrude_release", "trace", "total", "rank_fallbacks", "adjust_fallbacks",
                      "serial_chain_walks", "serial_contact_attempts", "fix_fallbacks", "refills",
                      "stale_refills", "epochs", "rank_pdq", "rank_pass", "rank_block",
-                     "rank_merge")
+                     "rank_merge", "rank_serial")
 
     def last_profile(self):
         buf = (C.c_uint64 * 32)()
