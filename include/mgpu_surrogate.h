@@ -61,10 +61,17 @@ int msur_conv_forward(const void* x, int B, int L, int Cin, const void* w, int C
  * msur_conv_get_stages returns the current depth (negative on a bad width). */
 int msur_conv_set_stages(int bn, int stages);
 int msur_conv_get_stages(int bn);
-/* Kernel form of msur_conv_forward for one N tile width: 0 = one CTA per output tile; 1 = a
- * persistent kernel (CTAs walk the tiles with a double-buffered TMEM accumulator, so a tile's
- * epilogue overlaps the next tile's MMAs).  Results are identical; the default is 0 and the
- * autotuner picks per device.  The getter returns the current form (negative on a bad width). */
+/* Kernel form of msur_conv_forward for one N tile width, two bits:
+ *   bit 0: a persistent kernel (CTAs walk the tiles with a double-buffered TMEM accumulator, so
+ *          a tile's epilogue overlaps the next tile's MMAs) instead of one CTA per output tile;
+ *   bit 1: the staged epilogue: each epilogue warp writes 32 rows x 64 columns of output to
+ *          shared memory and stores them with a TMA store, instead of one row per thread
+ *          (calls with a gate always take the per-thread epilogue).
+ * Results are identical in every form; the default is 2 and the autotuner picks per device and
+ * per layer.  The getter returns the current form (negative on a bad width).
+ * msur_conv_set_persistent / msur_conv_get_persistent set and read bit 0 alone. */
+int msur_conv_set_form(int bn, int form);
+int msur_conv_get_form(int bn);
 int msur_conv_set_persistent(int bn, int on);
 int msur_conv_get_persistent(int bn);
 

@@ -10,9 +10,10 @@
    unless it beats the engine's default (16 KiB, 60 %) by less than 5 %, the trials' spread, in
    which case the default stays.  The settings only move per-LEF arrays between
    shared memory and global slots, so every candidate simulates the same cells.
-2. Surrogate convolutions: the kernel form (one CTA per tile, or persistent) and pipeline depth
-   (2-4 stages) per N tile width of msur_conv_forward, then per forward layer of the network,
-   by coordinate descent on the network's inference time at batch 256.
+2. Surrogate convolutions: the kernel form (one CTA per tile or persistent, outputs per thread or
+   staged through shared memory and TMA stores) and pipeline depth (2-4 stages) per N tile width
+   of msur_conv_forward, then per forward layer of the network, by coordinate descent on the
+   network's inference time at batch 256.
 
 The result is a JSON file keyed by the device's name and SM count; ``load_table`` and
 ``apply_all`` read it back (engine contexts and the surrogate library take it from there).  The
@@ -140,22 +141,22 @@ def tune_surrogate(batch=256, reps=5):
         torch.cuda.synchronize()
         return ev0.elapsed_time(ev1) / reps
 
-    choice = {bn: (ops.conv_get_persistent(bn), ops.conv_get_stages(bn)) for bn in (64, 128, 256)}
+    choice = {bn: (ops.conv_get_form(bn), ops.conv_get_stages(bn)) for bn in (64, 128, 256)}
     trials = []
     base = timed()
     for _ in range(2):  # two rounds of coordinate descent over (kernel form, stages) per N tile
         for bn in (256, 128, 64):
             times = {}
-            for persistent in (0, 1):
+            for form in (0, 1, 2, 3):
                 for stages in (2, 3, 4):
-                    ops.conv_set_persistent(bn, persistent)
+                    ops.conv_set_form(bn, form)
                     ops.conv_set_stages(bn, stages)
-                    times[(persistent, stages)] = timed()
-                    trials.append({"bn": bn, "persistent": persistent, "stages": stages,
+                    times[(form, stages)] = timed()
+                    trials.append({"bn": bn, "form": form, "stages": stages,
                                    "others": {str(k): list(v) for k, v in choice.items()},
-                                   "ms_per_batch": times[(persistent, stages)]})
+                                   "ms_per_batch": times[(form, stages)]})
             choice[bn] = min(times, key=times.get)
-            ops.conv_set_persistent(bn, choice[bn][0])
+            ops.conv_set_form(bn, choice[bn][0])
             ops.conv_set_stages(bn, choice[bn][1])
             log(f"conv N tile {bn}: {times} -> {choice[bn]}")
     per_width = timed()
@@ -169,17 +170,17 @@ def tune_surrogate(batch=256, reps=5):
     cur = timed()
     for name in net.specs:
         times = {}
-        for persistent in (0, 1):
+        for form in (0, 1, 2, 3):
             for stages in (2, 3, 4):
-                S.LAYER_CFG[name] = (persistent, stages)
-                times[(persistent, stages)] = timed()
+                S.LAYER_CFG[name] = (form, stages)
+                times[(form, stages)] = timed()
         best_cfg = min(times, key=times.get)
         S.LAYER_CFG[name] = best_cfg
         trials.append({"layer": name, "times": {f"{k[0]},{k[1]}": v for k, v in times.items()}})
         log(f"layer {name}: -> {best_cfg} ({times[best_cfg]:.3f} ms)")
     best = timed()
     out = {"stages": {str(k): v[1] for k, v in choice.items()},
-           "persistent": {str(k): v[0] for k, v in choice.items()},
+           "form": {str(k): v[0] for k, v in choice.items()},
            "layers": {k: list(v) for k, v in S.LAYER_CFG.items()}, "ms_per_batch_default": base,
            "ms_per_batch_per_width": per_width, "ms_per_batch_tuned": best, "batch": batch}
     S.LAYER_CFG.clear()
@@ -222,8 +223,12 @@ def apply_surrogate(tuned):
     if tuned and tuned.get("surrogate"):
         for bn, stages in tuned["surrogate"]["stages"].items():
             ops.conv_set_stages(int(bn), int(stages))
-        for bn, on in tuned["surrogate"].get("persistent", {}).items():
-            ops.conv_set_persistent(int(bn), int(on))
+        if "form" in tuned["surrogate"]:
+            for bn, form in tuned["surrogate"]["form"].items():
+                ops.conv_set_form(int(bn), int(form))
+        else:  # tables written before the staged epilogue: bit 0 alone
+            for bn, on in tuned["surrogate"].get("persistent", {}).items():
+                ops.conv_set_form(int(bn), int(on))
         from . import surrogate as S
 
         S.LAYER_CFG.clear()

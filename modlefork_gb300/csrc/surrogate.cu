@@ -64,7 +64,13 @@ struct ConvArgs {
   bf16* out_post;      // value after the activation, or null
   float* out_f32;      // FP32 value before the activation, or null
   unsigned* err;
+  // staged epilogue (no gate): each epilogue warp writes its 32 rows of a 64-column unit to
+  // shared memory and stores them with TMA.  Maps over [B][L][n_valid] with row stride
+  // out_stride and 128-byte swizzled boxes of 32 rows: FP32 boxes of 32 columns, BF16 of 64.
+  CUtensorMap tm_f32, tm_pre, tm_post;
 };
+
+constexpr int STAGE_OUT_BYTES = 4 * 2 * 4096;  // four epilogue warps x two 4 KB buffers
 
 template <int BN>
 __host__ __device__ constexpr uint32_t tmem_cols() {
@@ -147,7 +153,100 @@ __device__ __forceinline__ void conv_epilogue_chunk(const ConvArgs& a, float (&v
   }
 }
 
-template <int BN, int STAGES>
+// One 32-row x 128-byte box goes through this warp's staging buffer (two 4 KB buffers used in
+// turn; nb counts the warp's stores).  stage_begin waits until the buffer's previous store has
+// read it; the lanes then write their rows with the 128-byte swizzle (16-byte unit k of row r at
+// unit k ^ (r % 8), which also keeps the eight lanes of each vector store on distinct banks);
+// stage_end makes the writes visible to the bulk-copy proxy and lane 0 issues the TMA store.
+__device__ __forceinline__ uint8_t* stage_begin(uint8_t* stg, int nb) {
+  if (nb >= 2 && (threadIdx.x & 31) == 0) umma::bulk_wait_read<1>();
+  __syncwarp();
+  return stg + (nb & 1) * 4096;
+}
+__device__ __forceinline__ void stage_put(uint8_t* buf, int k, uint4 w) {
+  const int lane = threadIdx.x & 31;
+  *reinterpret_cast<uint4*>(buf + lane * 128 + ((k ^ (lane & 7)) << 4)) = w;
+}
+__device__ __forceinline__ void stage_end(const CUtensorMap* map, uint8_t* buf, int& nb, int x, int y, int z) {
+  umma::fence_async_smem();
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) {
+    umma::tma_store_3d(map, buf, x, y, z);
+    umma::bulk_commit();
+  }
+  ++nb;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  const __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&p);
+}
+
+// Staged epilogue of one tile row block (32 rows y .. y+31 of sequence z, columns n0 .. n0+BN):
+// per 64-column unit, bias, then the FP32 (two boxes), pre-activation and post-activation (one
+// box each) outputs through shared memory and TMA.  Rows >= L and columns >= n_valid are dropped
+// by the stores.  Collective over the warp; the caller waits for the stores (bulk_wait_all)
+// before the block exits.
+template <int BN>
+__device__ void conv_epilogue_staged(const ConvArgs& a, uint32_t tmem_row, uint8_t* stg, int& nb, int n0, int y,
+                                     int z) {
+#pragma unroll 1
+  for (int u = 0; u < BN / 64; ++u) {
+    float v[64];
+    umma::tmem_ld32(tmem_row + u * 64, *reinterpret_cast<float(*)[32]>(v));
+    umma::tmem_ld32(tmem_row + u * 64 + 32, *reinterpret_cast<float(*)[32]>(v + 32));
+    const int col0 = n0 + u * 64;
+    if (y >= a.L || col0 >= a.n_valid) continue;
+    if (a.bias) {
+      const int nv = min(64, a.n_valid - col0);
+#pragma unroll
+      for (int j = 0; j < 64; ++j) v[j] += (j < nv) ? __ldg(a.bias + col0 + j) : 0.0f;
+    }
+    if (a.out_f32) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (col0 + 32 * h >= a.n_valid) break;
+        uint8_t* buf = stage_begin(stg, nb);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          stage_put(buf, k,
+                    make_uint4(__float_as_uint(v[32 * h + 4 * k]), __float_as_uint(v[32 * h + 4 * k + 1]),
+                               __float_as_uint(v[32 * h + 4 * k + 2]), __float_as_uint(v[32 * h + 4 * k + 3])));
+        stage_end(&a.tm_f32, buf, nb, col0 + 32 * h, y, z);
+      }
+    }
+    if (a.out_pre) {
+      uint8_t* buf = stage_begin(stg, nb);
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        stage_put(buf, k,
+                  make_uint4(pack_bf16x2(v[8 * k], v[8 * k + 1]), pack_bf16x2(v[8 * k + 2], v[8 * k + 3]),
+                             pack_bf16x2(v[8 * k + 4], v[8 * k + 5]), pack_bf16x2(v[8 * k + 6], v[8 * k + 7])));
+      stage_end(&a.tm_pre, buf, nb, col0, y, z);
+    }
+    if (a.out_post) {
+      if (a.act == MSUR_ACT_SILU) {
+#pragma unroll
+        for (int j = 0; j < 64; ++j) v[j] = silu(v[j]);
+      }
+      uint8_t* buf = stage_begin(stg, nb);
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        stage_put(buf, k,
+                  make_uint4(pack_bf16x2(v[8 * k], v[8 * k + 1]), pack_bf16x2(v[8 * k + 2], v[8 * k + 3]),
+                             pack_bf16x2(v[8 * k + 4], v[8 * k + 5]), pack_bf16x2(v[8 * k + 6], v[8 * k + 7])));
+      stage_end(&a.tm_post, buf, nb, col0, y, z);
+    }
+  }
+}
+
+// Every TMA store of this warp has completed (before the block and its shared memory exit).
+__device__ __forceinline__ void staged_drain() {
+  if ((threadIdx.x & 31) == 0) umma::bulk_wait_all();
+  __syncwarp();
+}
+
+template <int BN, int STAGES, bool STAGED>
 __global__ void __launch_bounds__(THREADS, 1) conv_fwd_kernel(const __grid_constant__ ConvArgs a) {
   constexpr int A_BYTES = BM * BK * 2;
   constexpr int B_BYTES = BN * BK * 2;
@@ -226,7 +325,14 @@ __global__ void __launch_bounds__(THREADS, 1) conv_fwd_kernel(const __grid_const
     const size_t row = static_cast<size_t>(b) * a.L + (row_ok ? l : 0);
     const bool ok = umma::mbar_wait(done, 0, a.err, ERR_EPILOGUE);
     umma::fence_after_sync();
-    if (ok) {
+    if constexpr (STAGED) {
+      if (ok) {
+        int nb = 0;
+        conv_epilogue_staged<BN>(a, tmem + (static_cast<uint32_t>(32 * q) << 16),
+                                 smem + STAGES * STAGE_BYTES + 1024 + q * 8192, nb, n0, l0 + 32 * q, b);
+        staged_drain();
+      }
+    } else if (ok) {
 #pragma unroll 1
       for (int c = 0; c < BN / 32; ++c) {
         float v[32];
@@ -253,7 +359,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_fwd_kernel(const __grid_const
 // Barriers: full / empty per smem stage (TMA <-> MMA), tfull / tempty per accumulator
 // (MMA <-> the 128 epilogue threads), done (the MMA issuer's last commit).
 // ---------------------------------------------------------------------------------------
-template <int BN, int STAGES>
+template <int BN, int STAGES, bool STAGED>
 __global__ void __launch_bounds__(THREADS, 1) conv_fwd_persistent_kernel(const __grid_constant__ ConvArgs a, int ntn,
                                                                          int ntl, int ntiles) {
   constexpr int A_BYTES = BM * BK * 2;
@@ -352,28 +458,35 @@ __global__ void __launch_bounds__(THREADS, 1) conv_fwd_persistent_kernel(const _
     }
   } else {
     const int q = warp & 3;
-    int j = 0;
+    int j = 0, nb = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++j) {
       const int acc = j & 1;
       const bool ok = umma::mbar_wait(&tfull[acc], (j >> 1) & 1, a.err, ERR_EPILOGUE);
       umma::fence_after_sync();
       if (!ok) break;
       const int n0 = (t % ntn) * BN;
-      const int l = ((t / ntn) % ntl) * BM + 32 * q + lane;
+      const int y = ((t / ntn) % ntl) * BM + 32 * q;
       const int b = t / (ntn * ntl);
-      const bool row_ok = l < a.L;
-      const size_t row = static_cast<size_t>(b) * a.L + (row_ok ? l : 0);
+      if constexpr (STAGED) {
+        conv_epilogue_staged<BN>(a, tmem + (static_cast<uint32_t>(32 * q) << 16) + acc * BN,
+                                 smem + STAGES * STAGE_BYTES + 1024 + q * 8192, nb, n0, y, b);
+      } else {
+        const int l = y + lane;
+        const bool row_ok = l < a.L;
+        const size_t row = static_cast<size_t>(b) * a.L + (row_ok ? l : 0);
 #pragma unroll 1
-      for (int c = 0; c < BN / 32; ++c) {
-        float v[32];
-        umma::tmem_ld32(tmem + (static_cast<uint32_t>(32 * q) << 16) + acc * BN + c * 32, v);
-        const int col0 = n0 + c * 32;
-        if (!row_ok || col0 >= a.n_valid) continue;
-        conv_epilogue_chunk(a, v, row, col0);
+        for (int c = 0; c < BN / 32; ++c) {
+          float v[32];
+          umma::tmem_ld32(tmem + (static_cast<uint32_t>(32 * q) << 16) + acc * BN + c * 32, v);
+          const int col0 = n0 + c * 32;
+          if (!row_ok || col0 >= a.n_valid) continue;
+          conv_epilogue_chunk(a, v, row, col0);
+        }
       }
       umma::fence_before_sync();
       umma::mbar_arrive(&tempty[acc]);
     }
+    if constexpr (STAGED) staged_drain();
   }
   umma::fence_before_sync();
   __syncthreads();
@@ -830,8 +943,11 @@ unsigned* g_dev_err[64] = {};
 // pipeline stages of the forward/data-gradient convolution per N tile width (64, 128, 256):
 // fewer stages let more CTAs share an SM, so one tile's epilogue overlaps another's main loop
 int g_conv_stages[3] = {4, 3, 4};
-// 1: the persistent kernel (double-buffered TMEM accumulator) for that N tile width
-int g_conv_persistent[3] = {0, 0, 0};
+// kernel form per N tile width: bit 0 the persistent kernel (double-buffered TMEM accumulator),
+// bit 1 the staged epilogue (outputs through shared memory and TMA stores)
+int g_conv_form[3] = {2, 2, 2};
+
+int conv_slot(int bn) { return bn == 256 ? 2 : (bn == 128 ? 1 : 0); }
 
 int fail(int code, const char* fmt, ...) {
   va_list ap;
@@ -890,10 +1006,32 @@ int make_map(CUtensorMap* m, const void* base, int rank, const uint64_t* dims, c
   return MSUR_OK;
 }
 
-template <int BN, int STAGES>
+// Output map of the staged epilogue: [B][L][n_valid] elements of elem_bytes with row stride
+// out_stride, boxes of box_x columns x 32 rows, 128-byte swizzle.
+int make_out_map(CUtensorMap* m, void* base, CUtensorMapDataType type, int elem_bytes, int n_valid, int out_stride,
+                 int L, int B, int box_x) {
+  const cuuint64_t gd[3] = {static_cast<cuuint64_t>(n_valid), static_cast<cuuint64_t>(L), static_cast<cuuint64_t>(B)};
+  const cuuint64_t gs[2] = {static_cast<cuuint64_t>(out_stride) * elem_bytes,
+                            static_cast<cuuint64_t>(out_stride) * elem_bytes * L};
+  const cuuint32_t bx[3] = {static_cast<cuuint32_t>(box_x), 32, 1}, es[3] = {1, 1, 1};
+  const CUresult r = g_encode(m, type, 3, base, gd, gs, bx, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                              CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(MSUR_ERR_CUDA, "cuTensorMapEncodeTiled (output) failed (%d)", static_cast<int>(r));
+  return MSUR_OK;
+}
+
+// Dynamic shared memory of a forward kernel: operand stages, alignment slack, the barriers (a
+// 1 KB block when the staged epilogue's buffers follow it).
+template <int BN, int STAGES, bool STAGED>
+constexpr int conv_smem() {
+  return STAGES * (BM * BK * 2 + BN * BK * 2) + 1024 + (STAGED ? 1024 + STAGE_OUT_BYTES : 256);
+}
+
+template <int BN, int STAGES, bool STAGED>
 int launch_conv(const ConvArgs& a, int ntiles_n, cudaStream_t st) {
-  constexpr int smem = STAGES * (BM * BK * 2 + BN * BK * 2) + 1024 + 256;
-  auto kern = conv_fwd_kernel<BN, STAGES>;
+  constexpr int smem = conv_smem<BN, STAGES, STAGED>();
+  auto kern = conv_fwd_kernel<BN, STAGES, STAGED>;
   int rc = cuda_ok(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem), "smem attribute");
   if (rc) return rc;
   dim3 grid(ntiles_n, (a.L + BM - 1) / BM, a.B);
@@ -901,11 +1039,11 @@ int launch_conv(const ConvArgs& a, int ntiles_n, cudaStream_t st) {
   return cuda_ok(cudaGetLastError(), "conv_fwd_kernel launch");
 }
 
-template <int BN, int STAGES>
+template <int BN, int STAGES, bool STAGED>
 int launch_conv_persistent(const ConvArgs& a, int ntn, cudaStream_t st) {
-  constexpr int smem = STAGES * (BM * BK * 2 + BN * BK * 2) + 1024 + 256;
+  constexpr int smem = conv_smem<BN, STAGES, STAGED>();
   constexpr int tcols = static_cast<int>(tmem_cols<2 * BN>());
-  auto kern = conv_fwd_persistent_kernel<BN, STAGES>;
+  auto kern = conv_fwd_persistent_kernel<BN, STAGES, STAGED>;
   int rc = cuda_ok(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem), "smem attribute");
   if (rc) return rc;
   int dev = 0, sms = 0, per_sm = 0;
@@ -919,6 +1057,22 @@ int launch_conv_persistent(const ConvArgs& a, int ntn, cudaStream_t st) {
   const int grid = std::min(ntiles, sms * per_sm);
   kern<<<grid, THREADS, smem, st>>>(a, ntn, ntl, ntiles);
   return cuda_ok(cudaGetLastError(), "conv_fwd_persistent_kernel launch");
+}
+
+template <int BN, int STAGES>
+int launch_conv_form(const ConvArgs& a, int ntn, bool persistent, bool staged, cudaStream_t st) {
+  if (persistent) {
+    return staged ? launch_conv_persistent<BN, STAGES, true>(a, ntn, st)
+                  : launch_conv_persistent<BN, STAGES, false>(a, ntn, st);
+  }
+  return staged ? launch_conv<BN, STAGES, true>(a, ntn, st) : launch_conv<BN, STAGES, false>(a, ntn, st);
+}
+
+template <int BN>
+int dispatch_conv(const ConvArgs& a, int ntn, bool persistent, bool staged, int stages, cudaStream_t st) {
+  if (stages == 2) return launch_conv_form<BN, 2>(a, ntn, persistent, staged, st);
+  if (stages == 3) return launch_conv_form<BN, 3>(a, ntn, persistent, staged, st);
+  return launch_conv_form<BN, 4>(a, ntn, persistent, staged, st);
 }
 
 template <int BN, int NT, int STAGES>
@@ -1000,34 +1154,23 @@ int msur_conv_forward(const void* x, int B, int L, int Cin, const void* w, int C
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int slot = BN == 256 ? 2 : (BN == 128 ? 1 : 0);
   const int stages = g_conv_stages[slot];
-  if (g_conv_persistent[slot]) {
-    if (BN == 256) {
-      if (stages == 2) return launch_conv_persistent<256, 2>(a, ntn, st);
-      if (stages == 3) return launch_conv_persistent<256, 3>(a, ntn, st);
-      return launch_conv_persistent<256, 4>(a, ntn, st);
-    }
-    if (BN == 128) {
-      if (stages == 2) return launch_conv_persistent<128, 2>(a, ntn, st);
-      if (stages == 4) return launch_conv_persistent<128, 4>(a, ntn, st);
-      return launch_conv_persistent<128, 3>(a, ntn, st);
-    }
-    if (stages == 2) return launch_conv_persistent<64, 2>(a, ntn, st);
-    if (stages == 3) return launch_conv_persistent<64, 3>(a, ntn, st);
-    return launch_conv_persistent<64, 4>(a, ntn, st);
+  // kernel form: bit 0 the persistent kernel, bit 1 the staged epilogue (outputs through shared
+  // memory and TMA), which needs no gate: the data gradient's gate is read row by row, so that
+  // epilogue stays per thread
+  const int form = g_conv_form[slot];
+  const bool persistent = (form & 1) != 0;
+  const bool staged = (form & 2) != 0 && !gate;
+  if (staged) {
+    if (out_f32) rc = make_out_map(&a.tm_f32, out_f32, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, n_valid, out_stride, L, B, 32);
+    if (!rc && out_pre)
+      rc = make_out_map(&a.tm_pre, out_pre, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, n_valid, out_stride, L, B, 64);
+    if (!rc && out_post)
+      rc = make_out_map(&a.tm_post, out_post, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, n_valid, out_stride, L, B, 64);
+    if (rc) return rc;
   }
-  if (BN == 256) {
-    if (stages == 2) return launch_conv<256, 2>(a, ntn, st);
-    if (stages == 3) return launch_conv<256, 3>(a, ntn, st);
-    return launch_conv<256, 4>(a, ntn, st);
-  }
-  if (BN == 128) {
-    if (stages == 2) return launch_conv<128, 2>(a, ntn, st);
-    if (stages == 4) return launch_conv<128, 4>(a, ntn, st);
-    return launch_conv<128, 3>(a, ntn, st);
-  }
-  if (stages == 2) return launch_conv<64, 2>(a, ntn, st);
-  if (stages == 3) return launch_conv<64, 3>(a, ntn, st);
-  return launch_conv<64, 4>(a, ntn, st);
+  if (BN == 256) return dispatch_conv<256>(a, ntn, persistent, staged, stages, st);
+  if (BN == 128) return dispatch_conv<128>(a, ntn, persistent, staged, stages, st);
+  return dispatch_conv<64>(a, ntn, persistent, staged, stages, st);
 }
 
 int msur_conv_set_stages(int bn, int stages) {
@@ -1038,16 +1181,30 @@ int msur_conv_set_stages(int bn, int stages) {
   return MSUR_OK;
 }
 
+int msur_conv_set_form(int bn, int form) {
+  if ((bn != 64 && bn != 128 && bn != 256) || form < 0 || form > 3)
+    return fail(MSUR_ERR_INVALID_ARG, "msur_conv_set_form: N tile 64, 128 or 256 and form 0 to 3");
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_conv_form[conv_slot(bn)] = form;
+  return MSUR_OK;
+}
+
+int msur_conv_get_form(int bn) {
+  if (bn != 64 && bn != 128 && bn != 256) return fail(MSUR_ERR_INVALID_ARG, "msur_conv_get_form: bad N tile");
+  return g_conv_form[conv_slot(bn)];
+}
+
 int msur_conv_set_persistent(int bn, int on) {
   if (bn != 64 && bn != 128 && bn != 256) return fail(MSUR_ERR_INVALID_ARG, "msur_conv_set_persistent: bad N tile");
   std::lock_guard<std::mutex> lk(g_mu);
-  g_conv_persistent[bn == 256 ? 2 : (bn == 128 ? 1 : 0)] = on ? 1 : 0;
+  int& f = g_conv_form[conv_slot(bn)];
+  f = (f & 2) | (on ? 1 : 0);
   return MSUR_OK;
 }
 
 int msur_conv_get_persistent(int bn) {
   if (bn != 64 && bn != 128 && bn != 256) return fail(MSUR_ERR_INVALID_ARG, "msur_conv_get_persistent: bad N tile");
-  return g_conv_persistent[bn == 256 ? 2 : (bn == 128 ? 1 : 0)];
+  return g_conv_form[conv_slot(bn)] & 1;
 }
 
 int msur_conv_get_stages(int bn) {

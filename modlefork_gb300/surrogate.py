@@ -35,8 +35,9 @@ NROWS = 600     # diagonals of the band (3 Mbp at 5 kb)
 HEAD_PAD = 640  # head channels: the 600 diagonals padded to the tile width
 IN_CH = 64      # input channels (8 used, padded to the tensor cores' K step)
 LOSS_SCALE = 1024.0
-# Tuned kernel form and pipeline depth per forward convolution, name -> (persistent, stages)
-# (filled from the autotuner's table by autotune.apply_surrogate; results do not depend on it).
+# Tuned kernel form (surrogate_ops.FORM_* bits) and pipeline depth per forward convolution,
+# name -> (form, stages) (filled from the autotuner's table by autotune.apply_surrogate; results
+# do not depend on it).
 LAYER_CFG = {}
 
 
@@ -206,7 +207,7 @@ class UNet:
         cfg = LAYER_CFG.get(name)
         if cfg is not None:
             bn = tile_width(s.cout)
-            ops.conv_set_persistent(bn, cfg[0])
+            ops.conv_set_form(bn, cfg[0])
             ops.conv_set_stages(bn, cfg[1])
         ops.conv_forward(x, self.wb[name], bias=self.b32[name], act=ops.ACT_SILU if s.act else ops.ACT_NONE,
                          out_pre=pre, out_post=post, out_f32=f32, **kw)

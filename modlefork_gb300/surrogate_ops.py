@@ -48,6 +48,8 @@ def load(path=LIB_PATH):
         "msur_compact_rows": (i32, [vp, i32, u64, i32, vp, vp]),
         "msur_conv_set_stages": (i32, [i32, i32]),
         "msur_conv_get_stages": (i32, [i32]),
+        "msur_conv_set_form": (i32, [i32, i32]),
+        "msur_conv_get_form": (i32, [i32]),
         "msur_conv_set_persistent": (i32, [i32, i32]),
         "msur_conv_get_persistent": (i32, [i32]),
     }
@@ -197,6 +199,19 @@ def conv_set_stages(bn, stages):
 
 def conv_get_stages(bn):
     return load().msur_conv_get_stages(bn)
+
+
+FORM_PERSISTENT = 1  # bit 0: persistent kernel instead of one CTA per tile
+FORM_STAGED = 2      # bit 1: outputs through shared memory and TMA stores
+
+
+def conv_set_form(bn, form):
+    """Kernel form (FORM_* bits, 0-3) of the convolution kernels with N tile bn (64, 128, 256)."""
+    _check(load().msur_conv_set_form(bn, form), "msur_conv_set_form")
+
+
+def conv_get_form(bn):
+    return load().msur_conv_get_form(bn)
 
 
 def conv_set_persistent(bn, on):

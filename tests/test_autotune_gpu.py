@@ -52,10 +52,12 @@ def test_launch_table_is_validated():
 
 @pytest.mark.parametrize("Cout,gated", [(64, False), (128, True), (256, False), (640, False), (384, True)])
 def test_conv_kernel_forms_and_depths_give_the_same_outputs(Cout, gated):
-    """The one-CTA-per-tile and the persistent kernel, at every pipeline depth, give bit-identical
-    results (each tile's MMAs run in the same order); the first form is checked against FP64 in
-    test_surrogate_kernels_gpu.py.  Shapes cover several tiles per CTA, ragged position tiles,
-    several sequences and the SiLU gate of the data gradient."""
+    """The one-CTA-per-tile and the persistent kernel, with per-thread or staged (shared memory
+    and TMA store) epilogues, at every pipeline depth, give bit-identical results (each tile's
+    MMAs run in the same order); the default form is checked against FP64 in
+    test_surrogate_kernels_gpu.py.  Shapes cover several tiles per CTA, ragged position tiles
+    (rows past the sequence end, which the TMA stores drop), several sequences and the SiLU gate
+    of the data gradient (which always takes the per-thread epilogue)."""
     rng = np.random.default_rng(Cout)
     B, L, Cin = 3, 1000, 128
     x = torch.from_numpy(rng.standard_normal((B, L, Cin)).astype(np.float32)).to("cuda", torch.bfloat16)
@@ -64,22 +66,24 @@ def test_conv_kernel_forms_and_depths_give_the_same_outputs(Cout, gated):
     gate = (torch.from_numpy(rng.standard_normal((B, L, Cout)).astype(np.float32)).to("cuda", torch.bfloat16)
             if gated else None)
     bn = 64 if Cout <= 64 else (256 if Cout % 256 == 0 else 128)
-    saved = (ops.conv_get_stages(bn), ops.conv_get_persistent(bn))
+    saved = (ops.conv_get_stages(bn), ops.conv_get_form(bn))
     outs = {}
     try:
-        for persistent in (0, 1):
+        for form in (0, 1, 2, 3):
             for stages in (2, 3, 4):
-                ops.conv_set_persistent(bn, persistent)
+                ops.conv_set_form(bn, form)
                 ops.conv_set_stages(bn, stages)
-                y = torch.empty(B, L, Cout, dtype=torch.float32, device="cuda")
-                post = torch.empty(B, L, Cout, dtype=torch.bfloat16, device="cuda")
-                ops.conv_forward(x, w, bias=bias, act=ops.ACT_SILU, out_f32=y, out_post=post, gate=gate)
-                outs[(persistent, stages)] = (y.cpu().numpy(), post.float().cpu().numpy())
+                y = torch.full((B, L, Cout), 7.0, dtype=torch.float32, device="cuda")
+                pre = torch.full((B, L, Cout), 7.0, dtype=torch.bfloat16, device="cuda")
+                post = torch.full((B, L, Cout), 7.0, dtype=torch.bfloat16, device="cuda")
+                ops.conv_forward(x, w, bias=bias, act=ops.ACT_SILU, out_f32=y, out_pre=pre, out_post=post,
+                                 gate=gate)
+                outs[(form, stages)] = (y.cpu().numpy(), pre.float().cpu().numpy(), post.float().cpu().numpy())
     finally:
         ops.conv_set_stages(bn, saved[0])
-        ops.conv_set_persistent(bn, saved[1])
+        ops.conv_set_form(bn, saved[1])
     torch.cuda.synchronize()
     assert ops.take_error() == 0
     want = outs[(0, 2)]
-    for k, (y, post) in outs.items():
-        assert np.array_equal(y, want[0]) and np.array_equal(post, want[1]), k
+    for k, got in outs.items():
+        assert all(np.array_equal(g, w_) for g, w_ in zip(got, want)), k

@@ -180,6 +180,15 @@ def test_launch_setting_layout_and_surrogate_library_exports():
         surrogate_ops.conv_set_stages(128, 5)
     for bn, default in ((64, 4), (128, 3), (256, 4)):
         assert surrogate_ops.conv_get_stages(bn) == default
+        assert surrogate_ops.conv_get_form(bn) == surrogate_ops.FORM_STAGED
         assert surrogate_ops.conv_get_persistent(bn) == 0
     with pytest.raises(surrogate_ops.SurrogateKernelError):
         surrogate_ops.conv_set_persistent(32, 1)
+    for bad in ((32, 0), (128, 4), (128, -1)):
+        with pytest.raises(surrogate_ops.SurrogateKernelError):
+            surrogate_ops.conv_set_form(*bad)
+    # the persistent bit alone, then back
+    surrogate_ops.conv_set_persistent(128, 1)
+    assert surrogate_ops.conv_get_form(128) == 3 and surrogate_ops.conv_get_persistent(128) == 1
+    surrogate_ops.conv_set_form(128, surrogate_ops.FORM_STAGED)
+    assert surrogate_ops.conv_get_persistent(128) == 0

@@ -70,20 +70,20 @@ def test_shipped_per_layer_tuning_names_every_convolution():
 
     table = json.load(open(autotune.DEFAULT_FILE))["devices"]
     names = [s.name for s in surrogate.conv_specs((64, 128, 256, 384, 512), 512)]
-    saved = {bn: (surrogate_ops.conv_get_persistent(bn), surrogate_ops.conv_get_stages(bn)) for bn in (64, 128, 256)}
+    saved = {bn: (surrogate_ops.conv_get_form(bn), surrogate_ops.conv_get_stages(bn)) for bn in (64, 128, 256)}
     try:
         for tuned in table.values():
             layers = tuned["surrogate"]["layers"]
             assert sorted(layers) == sorted(names)
-            assert all(p in (0, 1) and s in (2, 3, 4) for p, s in layers.values())
+            assert all(f in (0, 1, 2, 3) and s in (2, 3, 4) for f, s in layers.values())
             autotune.apply_surrogate(tuned)
             assert surrogate.LAYER_CFG == {k: tuple(v) for k, v in layers.items()}
             for bn, stages in tuned["surrogate"]["stages"].items():
                 assert surrogate_ops.conv_get_stages(int(bn)) == stages
     finally:
         surrogate.LAYER_CFG.clear()
-        for bn, (p, s) in saved.items():
-            surrogate_ops.conv_set_persistent(bn, p)
+        for bn, (f, s) in saved.items():
+            surrogate_ops.conv_set_form(bn, f)
             surrogate_ops.conv_set_stages(bn, s)
     assert {surrogate.tile_width(c) for c in (64, 128, 256, 384, 512, 640)} == {64, 128, 256}
 
