@@ -42,9 +42,11 @@ enum : unsigned { ERR_PRODUCER = 1u, ERR_MMA = 2u, ERR_EPILOGUE = 4u };
 __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
   return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
 }
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+// SiLU and its derivative with the fast reciprocal-based division (within 2 ulp; the result is
+// 0 when 1 + exp(-z) overflows, the limit of both): the epilogues evaluate one per output element.
+__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 __device__ __forceinline__ float dsilu(float z) {
-  const float s = 1.0f / (1.0f + __expf(-z));
+  const float s = __fdividef(1.0f, 1.0f + __expf(-z));
   return s * (1.0f + z * (1.0f - s));
 }
 
@@ -199,8 +201,20 @@ __device__ void conv_epilogue_staged(const ConvArgs& a, uint32_t tmem_row, uint8
     if (y >= a.L || col0 >= a.n_valid) continue;
     if (a.bias) {
       const int nv = min(64, a.n_valid - col0);
+      if (nv == 64 && (reinterpret_cast<uintptr_t>(a.bias) & 15u) == 0) {
+        const float4* b4 = reinterpret_cast<const float4*>(a.bias + col0);
 #pragma unroll
-      for (int j = 0; j < 64; ++j) v[j] += (j < nv) ? __ldg(a.bias + col0 + j) : 0.0f;
+        for (int k = 0; k < 16; ++k) {
+          const float4 bb = __ldg(b4 + k);
+          v[4 * k] += bb.x;
+          v[4 * k + 1] += bb.y;
+          v[4 * k + 2] += bb.z;
+          v[4 * k + 3] += bb.w;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 64; ++j) v[j] += (j < nv) ? __ldg(a.bias + col0 + j) : 0.0f;
+      }
     }
     if (a.out_f32) {
 #pragma unroll

@@ -114,12 +114,14 @@ def simulate_genome(cfg, genome, ncells=None, device=0, simulate_wo_barriers=Fal
         raise errors[0]
     return [results[i] for i, _, _ in jobs]
 
-def simulate_genome_batched(cfg, genome, ncells=None, device=0, simulate_wo_barriers=False, cell_range=None):
+def simulate_genome_batched(cfg, genome, ncells=None, device=0, simulate_wo_barriers=False, cell_range=None,
+                            smem_budget=None, carveout=None):
     """simulate_genome with every chromosome's cells in one batched launch (mgpu_simulate_batch):
     one persistent kernel and one work queue for the whole genome, largest chromosomes first.
     Same results as one launch per chromosome.  cell_range = (lo, hi) simulates only cell ids
     lo .. hi - 1 of each chromosome (one rank's share); their seeds and targets are those of the
-    full run."""
+    full run.  smem_budget (bytes per cell) and carveout (percent of the SM's unified memory as
+    shared memory) replace the tuned launch table's choice when given."""
     ncells = int(cfg.num_cells if ncells is None else ncells)
     lo, hi = cell_range if cell_range is not None else (0, ncells)
     jobs = [(c, b) for c, b in genome if b or simulate_wo_barriers]
@@ -127,6 +129,8 @@ def simulate_genome_batched(cfg, genome, ncells=None, device=0, simulate_wo_barr
 
     with engine.Engine(cfg, device) as eng:
         autotune.apply_all(eng)
+        if smem_budget is not None or carveout is not None:
+            eng.set_debug_flags((int(carveout or 0) & 0xFF) << 8, int(smem_budget or 0))
         preps, tasks, bands = [], [], {}
         for chrom, barriers in jobs:
             t = prepare_chrom(eng, cfg, chrom, barriers, ncells)
@@ -251,6 +255,8 @@ def _main(argv=None):
     ap.add_argument("--workers", type=int, default=1, help="concurrent chromosome launches")
     ap.add_argument("--batched", action="store_true", help="all chromosomes in one batched launch")
     ap.add_argument("--smem-budget", type=int, default=None, help="shared memory per cell (bytes)")
+    ap.add_argument("--carveout", type=int, default=None,
+                    help="batched launch: percent of the SM's unified memory used as shared memory")
     ap.add_argument("--pixels", default=None, help="write the pixel table (bin1_id, bin2_id, count) as TSV")
     ap.add_argument("--lef-occupancy", default=None,
                     help="track the 1D LEF occupancy, write it as bigWig (.bw, .bigwig) or bedGraph")
@@ -266,7 +272,8 @@ def _main(argv=None):
     cfg.log_model_internal_state = 1 if args.model_state else 0
     t0 = time.perf_counter()
     if args.batched:
-        res = simulate_genome_batched(cfg, g, device=args.device)
+        res = simulate_genome_batched(cfg, g, device=args.device, smem_budget=args.smem_budget,
+                                      carveout=args.carveout)
     else:
         res = simulate_genome(cfg, g, device=args.device, workers=args.workers, smem_budget=args.smem_budget)
     dt = time.perf_counter() - t0

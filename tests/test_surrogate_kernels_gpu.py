@@ -76,8 +76,20 @@ CONV_SHAPES = [
 ]
 
 
+@pytest.fixture(params=[0, 1, 2, 3], ids=["tile", "persistent", "tile-staged", "persistent-staged"])
+def conv_form(request):
+    """Every kernel form of msur_conv_forward (per-thread or staged epilogue, one CTA per tile or
+    persistent) for all N tile widths, restored afterwards."""
+    saved = {bn: ops.conv_get_form(bn) for bn in (64, 128, 256)}
+    for bn in saved:
+        ops.conv_set_form(bn, request.param)
+    yield request.param
+    for bn, f in saved.items():
+        ops.conv_set_form(bn, f)
+
+
 @pytest.mark.parametrize("B,L,Cin,Cout,taps", CONV_SHAPES)
-def test_conv_forward_matches_fp64(B, L, Cin, Cout, taps):
+def test_conv_forward_matches_fp64(B, L, Cin, Cout, taps, conv_form):
     rng = np.random.default_rng(B * 1000 + L + Cin + Cout)
     xb = _bf16(rng.standard_normal((B, L, Cin)))
     wb = _bf16(rng.standard_normal((Cout, taps, Cin)) / np.sqrt(taps * Cin))
@@ -95,19 +107,22 @@ def test_conv_forward_matches_fp64(B, L, Cin, Cout, taps):
     _close(_np(post), _silu(ref), True)
 
 
-def test_conv_forward_head_masks_padded_channels():
-    """The output head: one tap, 640 weight rows of which 600 are written, FP32, row stride 600."""
+def test_conv_forward_head_masks_padded_channels(conv_form):
+    """The output head: one tap, 640 weight rows of which 600 are written, FP32, row stride 600;
+    the buffer's guard value must survive beyond the 600 columns of the last row."""
     rng = np.random.default_rng(11)
     B, L, Cin, N, NV = 2, 260, 64, 640, 600
     xb = _bf16(rng.standard_normal((B, L, Cin)))
     wb = _bf16(rng.standard_normal((N, 1, Cin)) / 8)
     bias = (rng.standard_normal(N) * 0.1).astype(np.float32)
-    out = torch.full((B, L, NV), 7.0, dtype=torch.float32, device=DEV)
+    buf = torch.full((B * L * NV + 64,), 7.0, dtype=torch.float32, device=DEV)
+    out = buf[:B * L * NV].view(B, L, NV)
     ops.conv_forward(xb.to(DEV), wb.to(DEV), bias=torch.from_numpy(bias).to(DEV), out_f32=out, n_valid=NV,
                      out_stride=NV)
     torch.cuda.synchronize()
     ref = _conv_ref(_np(xb), _np(wb), bias.astype(np.float64))[:, :, :NV]
     _close(_np(out), ref, False)
+    assert torch.all(buf[B * L * NV:] == 7.0)
 
 
 def test_data_gradient_through_silu_gate():
