@@ -212,8 +212,9 @@ class UNet:
         ops.conv_forward(x, self.wb[name], bias=self.b32[name], act=ops.ACT_SILU if s.act else ops.ACT_NONE,
                          out_pre=pre, out_post=post, out_f32=f32, **kw)
 
-    def forward(self, x, train=False):
-        """x: [B, L, 64] BF16 input; returns the [B, L, 600] FP32 prediction (a workspace view)."""
+    def forward(self, x, train=False, out=None):
+        """x: [B, L, 64] BF16 input; returns the [B, L, 600] FP32 prediction: `out` when given
+        (contiguous FP32 on the device), else a workspace view that the next call overwrites."""
         B = x.shape[0]
         ws = self._workspace(B, train)
         get = (lambda k: ws.get(k)) if train else (lambda k: None)
@@ -232,8 +233,9 @@ class UNet:
             self._conv(f"dec{i}a", ws[f"cat{i}"], pre=get(f"zda{i}"), post=ws[f"yda{i}"])
             self._conv(f"dec{i}b", ws[f"yda{i}"], pre=get(f"zdb{i}"), post=ws[f"ydb{i}"])
             h = ws[f"ydb{i}"]
-        self._conv("head", h, f32=ws["out"], n_valid=NROWS, out_stride=NROWS)
-        return ws["out"]
+        dst = ws["out"] if out is None else out
+        self._conv("head", h, f32=dst, n_valid=NROWS, out_stride=NROWS)
+        return dst
 
     # ---- backward ------------------------------------------------------------------------
     def _grads(self, name, x, dz):
@@ -356,6 +358,46 @@ def predict(net, x, batch=256):
     for i in range(0, x.shape[0], batch):
         j = min(x.shape[0], i + batch)
         out[i:j].copy_(net.forward(x[i:j], train=False))
+    return out
+
+
+def predict_host(net, track, params, out, batch=256):
+    """Host inputs in, host predictions out: track [N, 4, L] and params [N, 4] FP32 host tensors,
+    out [N, L, 600] FP32 host tensor (pinned memory, so that the copies run asynchronously).
+    Batches alternate between two device input/output slots: batch i's forward runs on the
+    current stream while batch i-1's predictions are copied back on a second stream, so the
+    device-to-host copy of the maps (9.6 MB each) overlaps the next batch's compute."""
+    N = track.shape[0]
+    dev = net.dev
+    compute = torch.cuda.current_stream(dev)
+    copier = torch.cuda.Stream(device=dev)
+    nb = min(batch, N)
+    slots = []
+    for _ in range(2):
+        slots.append({"track": torch.empty((nb,) + tuple(track.shape[1:]), dtype=torch.float32, device=dev),
+                      "params": torch.empty((nb,) + tuple(params.shape[1:]), dtype=torch.float32, device=dev),
+                      "x": torch.empty(nb, net.length, IN_CH, dtype=torch.bfloat16, device=dev),
+                      "out": torch.empty(nb, net.length, NROWS, dtype=torch.float32, device=dev),
+                      "copied": None})
+    for k, i in enumerate(range(0, N, batch)):
+        j = min(N, i + batch)
+        sl = slots[k % 2]
+        if sl["copied"] is not None:
+            compute.wait_event(sl["copied"])  # the slot's previous maps have left the device
+        n = j - i
+        sl["track"][:n].copy_(track[i:j], non_blocking=True)
+        sl["params"][:n].copy_(params[i:j], non_blocking=True)
+        ops.assemble_input(sl["track"][:n], sl["params"][:n], sl["x"][:n])
+        net.forward(sl["x"][:n], out=sl["out"][:n])
+        done = torch.cuda.Event()
+        done.record(compute)
+        copier.wait_event(done)
+        with torch.cuda.stream(copier):
+            out[i:j].copy_(sl["out"][:n], non_blocking=True)
+            sl["out"].record_stream(copier)
+            sl["copied"] = torch.cuda.Event()
+            sl["copied"].record(copier)
+    compute.wait_stream(copier)
     return out
 
 

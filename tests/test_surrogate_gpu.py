@@ -85,6 +85,23 @@ def test_full_size_forward_matches_the_fp64_oracle():
     _agree(out, want, "network output")
 
 
+def test_host_prediction_path_equals_device_prediction():
+    """predict_host (host inputs, host outputs, batches alternating between two device slots with
+    the copies back on a second stream, a short last batch) gives the maps predict gives from
+    the same inputs assembled on the device, bit for bit."""
+    rng = np.random.default_rng(8)
+    net = S.UNet(seed=3, head_bias=np.linspace(2, 0, S.NROWS))
+    N = 5
+    track = rng.random((N, 4, net.length)).astype(np.float32)
+    params = rng.random((N, 4)).astype(np.float32)
+    data = S.Dataset(track, params, np.zeros((N, net.length, S.NROWS), np.float32), net.dev)
+    want = S.predict(net, data.x, batch=2).cpu()
+    out = torch.full((N, net.length, S.NROWS), 7.0).pin_memory()
+    S.predict_host(net, torch.from_numpy(track).pin_memory(), torch.from_numpy(params).pin_memory(), out, batch=2)
+    torch.cuda.synchronize()
+    assert torch.equal(out, want)
+
+
 def test_training_lowers_the_loss():
     rng = np.random.default_rng(3)
     N, L = 12, 256
