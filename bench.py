@@ -54,7 +54,8 @@ def parse_args():
     ap.add_argument("--wave", type=int, default=24, help="chromosome launches per step")
     ap.add_argument("--smem-budget", type=int, default=None, help="shared memory per cell (bytes)")
     ap.add_argument("--carveout", type=int, default=None, help="shared-memory carveout percent")
-    ap.add_argument("--batched", type=int, default=1, help="also time the one-launch batched engine")
+    ap.add_argument("--wave-steps", type=int, default=1,
+                    help="timed steps of the plain path (one-chromosome launches from concurrent contexts)")
     ap.add_argument("--windows", type=int, default=16,
                     help="windows of the batched uneven-window workload timed in one launch (0 = skip)")
     ap.add_argument("--surrogate", type=int, default=1, help="also time the learned surrogate against the simulator")
@@ -240,6 +241,15 @@ def run_surrogate(args, log):
     S.predict_host(net, pin_track, pin_params, pin_out, batch=B)
     torch.cuda.synchronize()
     e2e_mps = B * nbatch / (time.perf_counter() - t0)
+    # the link that bounds it: one batch of maps copied device-to-host into the same pinned buffer
+    # (its rate depends on where the host placed the pinned pages, which varies between runs)
+    d_maps = torch.empty(B, net.length, S.NROWS, dtype=torch.float32, device=net.dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pin_out[:B].copy_(d_maps, non_blocking=True)
+    torch.cuda.synchronize()
+    d2h_gbs = d_maps.numel() * 4 / (time.perf_counter() - t0) / 1e9
+    del d_maps
     passed = r >= 0.95
     tpeak, tkind = measured_peak("bf16_tflops")
     eff = 1.0 / (1.0 / mps + (1.0 - passed.mean()) / sim_mps)
@@ -252,7 +262,8 @@ def run_surrogate(args, log):
         "simulator_config": "20 Mbp windows of the sweep generator, 1024 cells, contact density 10, one batched "
                             "launch (CUDA events around the launch)",
         "fp64_target_check_max_rel_dev": sims["fp64_max_rel_dev"],
-        "e2e": {"value": e2e_mps, "unit": "maps/s", "batches": nbatch,
+        "e2e": {"value": e2e_mps, "unit": "maps/s", "batches": nbatch, "d2h_gb_per_s": d2h_gbs,
+                "d2h_bound_maps_per_s": d2h_gbs * 1e9 / (net.length * S.NROWS * 4),
                 "h2d_bytes_per_step": int((pin_track.numel() + pin_params.numel()) * 4) // nbatch,
                 "d2h_bytes_per_step": int(pin_out.numel() * 4) // nbatch},
         "roofline": {"bound": "tensor", "achieved": tf, "peak": tpeak, "unit": "TFLOP/s", "frac": tf / tpeak,
@@ -495,30 +506,48 @@ def run_ours(args):
             agg["launches"] += 1
         return agg
 
+    # ---- headline: the whole genome in one batched launch per step (mgpu_simulate_batch) -------
+    # One persistent kernel and one work queue over every chromosome's cells, largest first: the
+    # GB300 form of the reference's task queue of (chromosome, cell) tasks over worker threads.
+    w0 = workers[0]
+    w0["eng"].set_debug_flags(0, 0)
+    tuning = autotune.apply_all(w0["eng"])
+    btasks = [(w0["cids"][k], int(sd), int(tg), t["te"], t["nlefs"])
+              for k, t in enumerate(tasks) for sd, tg in zip(t["seeds"], t["targets"])]
+    dbands = {w0["cids"][k]: t["d_band"].data_ptr() for k, t in enumerate(tasks)}
+
+    def batched_tally(bst):
+        agg = dict(lef_epochs=0, cells=len(bst), contacts=0, bytes=0, launches=1)
+        off = 0
+        for t in tasks:
+            st = bst[off:off + len(t["seeds"])]
+            agg["lef_epochs"] += sum(x.lef_epochs for x in st)
+            agg["contacts"] += sum(x.contacts for x in st)
+            agg["bytes"] += algorithmic_bytes(st, len(t["bars"]))
+            off += len(t["seeds"])
+        return agg
+
     for i in range(args.warmup):
         log(f"warm-up step {i}")
-        run_wave(i, True)
+        w0["eng"].simulate_batch(btasks, dbands)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    main = torch.cuda.current_stream()
     clocks = Clocks(local)
     clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(main)
-    for w in workers:
-        w["stream"].wait_event(ev0)
-    done = []
+    ev0.record(w0["stream"])
+    first_step, agg = None, dict(lef_epochs=0, cells=0, contacts=0, bytes=0, launches=0)
     for i in range(args.steps):
         log(f"timed step {i}")
-        done += run_wave(i, True)
-    for w in workers:
-        main.wait_stream(w["stream"])
-    ev1.record(main)
+        _, bst = w0["eng"].simulate_batch(btasks, dbands)
+        first_step = first_step if first_step is not None else bst
+        for key, v in batched_tally(bst).items():
+            agg[key] += v
+    ev1.record(w0["stream"])
     torch.cuda.synchronize()
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1)
-    agg = tally(done)
     log(f"timed region: {ms:.1f} ms")
     if world > 1:
         from modlefork_gb300 import sharding
@@ -527,72 +556,70 @@ def run_ours(args):
                                                                     "launches")}, device=dev)
         agg.update(sums)
         torch.distributed.barrier()
+    done = []  # (chromosome, stats) of the first timed step, for the parity check
+    off = 0
+    for k, t in enumerate(tasks):
+        done.append((k, first_step[off:off + len(t["seeds"])], 0.0))
+        off += len(t["seeds"])
 
     # end to end through the C ABI with host buffers (copies inside the timed region)
     e2e = None
     if args.e2e_steps > 0:
-        for t in tasks:
-            t["h_band"] = np.zeros(t["nrows"] * t["ncols"], dtype=np.uint32)
+        hb = {w0["cids"][k]: np.zeros(t["nrows"] * t["ncols"], dtype=np.uint32) for k, t in enumerate(tasks)}
         torch.cuda.synchronize()
-        edone, step_rates, dt = [], [], 0.0
+        step_rates, dt, ele, ecells = [], 0.0, 0, 0
         for i in range(args.e2e_steps):
             log(f"e2e step {i}")
+            for b in hb.values():
+                b[:] = 0
             t0 = time.perf_counter()
-            sdone = run_wave(i, False)
+            _, est = w0["eng"].simulate_batch(btasks, hb)
             torch.cuda.synchronize()
             sdt = time.perf_counter() - t0
             dt += sdt
-            step_rates.append(tally(sdone)["lef_epochs"] / sdt)
-            edone += sdone
-        eagg = tally(edone)
-        h2d = sum(tasks[k]["seeds"].nbytes + tasks[k]["targets"].nbytes + tasks[k]["h_band"].nbytes
-                  for k, _, _ in edone)
-        d2h = sum(tasks[k]["h_band"].nbytes + len(st) * C.sizeof(st[0]) for k, st, _ in edone)
-        e2e = {"value": eagg["lef_epochs"] / dt, "unit": "LEF-epochs/s",
-               "h2d_bytes_per_step": h2d // args.e2e_steps, "d2h_bytes_per_step": d2h // args.e2e_steps,
-               "steps": args.e2e_steps, "cells_per_s": eagg["cells"] / dt,
+            sle = sum(x.lef_epochs for x in est)
+            step_rates.append(sle / sdt)
+            ele += sle
+            ecells += len(est)
+        e2e = {"value": ele / dt, "unit": "LEF-epochs/s",
+               "h2d_bytes_per_step": int(sum(b.nbytes for b in hb.values()) + len(btasks) * 40),
+               "d2h_bytes_per_step": int(sum(b.nbytes for b in hb.values()) + len(btasks) * 64),
+               "steps": args.e2e_steps, "cells_per_s": ecells / dt,
                "step_rates": {"min": min(step_rates), "median": statistics.median(step_rates),
                               "max": max(step_rates)},
-               "timing": "host clock around each step's C-ABI calls and a device synchronisation"}
+               "timing": "host clock around each step's C-ABI call (task list, band buffers and per-cell "
+                         "stats copied in and out inside it) and a device synchronisation"}
 
-    # batched: the whole genome in one launch and work queue (mgpu_simulate_batch)
-    batched = None
-    if args.batched:
-        w0 = workers[0]
-        w0["eng"].set_debug_flags(0, 0)
-        tuning = autotune.apply_all(w0["eng"])
-        btasks = [(w0["cids"][k], int(sd), int(tg), t["te"], t["nlefs"])
-                  for k, t in enumerate(tasks) for sd, tg in zip(t["seeds"], t["targets"])]
-        dbands = {w0["cids"][k]: t["d_band"].data_ptr() for k, t in enumerate(tasks)}
-        log("batched warm-up")
-        w0["eng"].simulate_batch([x for x in btasks if x[0] in set(list(dbands)[:4])],
-                                 {c: dbands[c] for c in list(dbands)[:4]})
+    # the plain path: one-chromosome launches (mgpu_simulate_cells) from concurrent contexts
+    wave_line = None
+    if args.wave_steps > 0:
+        for w in workers:
+            w["eng"].set_debug_flags((carveout & 0xFF) << 8, budget)
+        log("plain wave warm-up")
+        run_wave(0, True)
         torch.cuda.synchronize()
-        log("batched timed launch")
-        bev0, bev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        bev0.record(w0["stream"])
-        _, bst = w0["eng"].simulate_batch(btasks, dbands)
-        bev1.record(w0["stream"])
+        main = torch.cuda.current_stream()
+        wev0, wev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        wev0.record(main)
+        for w in workers:
+            w["stream"].wait_event(wev0)
+        wdone = []
+        for i in range(args.wave_steps):
+            log(f"plain wave step {i}")
+            wdone += run_wave(i, True)
+        for w in workers:
+            main.wait_stream(w["stream"])
+        wev1.record(main)
         torch.cuda.synchronize()
-        bms = bev0.elapsed_time(bev1)
-        ble = sum(x.lef_epochs for x in bst)
-        bbytes, off = 0, 0
-        for t in tasks:
-            bbytes += algorithmic_bytes(bst[off:off + len(t["seeds"])], len(t["bars"]))
-            off += len(t["seeds"])
-        hb = {w0["cids"][k]: np.zeros(t["nrows"] * t["ncols"], dtype=np.uint32) for k, t in enumerate(tasks)}
-        log("batched end to end")
-        t0 = time.perf_counter()
-        _, bst2 = w0["eng"].simulate_batch(btasks, hb)
-        bdt = time.perf_counter() - t0
-        batched = {"value": ble / (bms / 1e3), "unit": "LEF-epochs/s", "ms": bms, "launches": 1,
-                   "cells_per_s": len(bst) / (bms / 1e3),
-                   "config": "the same 24 chromosomes x 512 cells in one batched launch, launch settings "
-                             + ("from the tuned table (modlefork_gb300/data/tuning_gb300.json)" if tuning
-                                else "16 KiB per cell, 60% carveout"),
-                   "e2e": {"value": sum(x.lef_epochs for x in bst2) / bdt, "unit": "LEF-epochs/s",
-                           "h2d_bytes_per_step": int(sum(b.nbytes for b in hb.values()) + len(btasks) * 40),
-                           "d2h_bytes_per_step": int(sum(b.nbytes for b in hb.values()) + len(btasks) * 64)}}
+        wms = wev0.elapsed_time(wev1)
+        wagg = tally(wdone)
+        wave_line = {"value": wagg["lef_epochs"] / (wms / 1e3), "unit": "LEF-epochs/s", "steps": args.wave_steps,
+                     "warmup": 1, "ms_per_step": wms / args.wave_steps, "cells_per_s": wagg["cells"] / (wms / 1e3),
+                     "launches": int(wagg["launches"]),
+                     "step": f"one wave of {wave} one-chromosome launches ({args.cells} cells each) over "
+                             f"{args.workers} concurrent contexts",
+                     "smem_budget_per_cell": budget, "smem_carveout_pct": carveout,
+                     "bytes": wagg["bytes"], "ms": wms}
 
     # the plain path one launch at a time: one context, every n-th chromosome's 512 cells in
     # one blocking call after another (the reference's drop-in used from a single worker), and
@@ -638,29 +665,17 @@ def run_ours(args):
         return
     peak, peak_kind = measured_peak()
     achieved = agg["bytes"] / (ms / 1e3) / 1e9
-    traffic, tinfo = dram_traffic_per_launch(agg["lef_epochs"] / max(1, agg["launches"]))
-    if batched is not None:
-        bach = bbytes / (batched["ms"] / 1e3) / 1e9
-        btraffic, _ = dram_traffic_per_launch(ble, "simulate_batch_kernel")
-        batched["roofline"] = {
-            "bound": "hbm", "achieved": bach, "peak": peak, "unit": "GB/s", "frac": bach / peak,
-            "traffic": btraffic, "peak_source": f"{peak_kind} hbm_gbs", "kernel": "simulate_batch_kernel",
-            "traffic_note": "DRAM bytes of the launch: ncu bytes per LEF-epoch of a one-wave batched "
-                            "launch (profiles/simulate_batch_kernel_traffic.json) x this launch's "
-                            "LEF-epochs; above the algorithmic bytes because the resident cells' arrays "
-                            "exceed L2"}
-    timed = sorted({(i * wave + j) % len(tasks) for i in range(args.steps) for j in range(wave)})
+    traffic, tinfo = dram_traffic_per_launch(agg["lef_epochs"] / max(1, agg["launches"]), "simulate_batch_kernel")
     line = {
         "metric": "LEF-epochs/s", "value": agg["lef_epochs"] / (ms / 1e3), "unit": "LEF-epochs/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32+f64",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "chromosomes": len(tasks), "cells_per_chromosome": args.cells,
-                   "step": f"one wave of {wave} one-chromosome launches ({args.cells} cells each) over "
-                           f"{args.workers} concurrent contexts; step i covers chromosomes "
-                           f"{wave}i..{wave}i+{wave - 1} mod {len(tasks)}",
-                   "timed_chromosomes": [tasks[k]["chrom"].name for k in timed],
-                   "workers": args.workers, "smem_budget_per_cell": budget, "smem_carveout_pct": carveout,
+                   "step": f"one batched launch (mgpu_simulate_batch) of all {len(tasks)} chromosomes x "
+                           f"{args.cells} cells, one work queue, largest chromosomes first",
+                   "launch_settings": ("the tuned table (modlefork_gb300/data/tuning_gb300.json)" if tuning
+                                       else "16 KiB per cell, 60% carveout"),
                    "genome_bp": int(sum(t["chrom"].size for t in tasks)),
                    "lefs": int(sum(t["nlefs"] for t in tasks)),
                    "barriers": int(sum(len(t["bars"]) for t in tasks)),
@@ -670,23 +685,28 @@ def run_ours(args):
         "gpu_launches": int(agg["launches"]),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "peak_source": f"{peak_kind} hbm_gbs", "kernel": "simulate_kernel",
-                     "bytes_model": "24*LEF_epochs + 6*barriers*epochs + 8*contacts, summed over the "
-                                    "launches of the timed region / region time (launches overlap)",
-                     "traffic_note": "DRAM bytes per launch: ncu bytes per LEF-epoch of one launch that "
-                                     "fills every SM with 24 KiB cells as the concurrent wave does "
-                                     "(profiles/simulate_kernel_traffic.json, 1064 resident cells of "
-                                     "chr11) x this run's LEF-epochs per launch",
+                     "peak_source": f"{peak_kind} hbm_gbs", "kernel": "simulate_batch_kernel",
+                     "bytes_model": "24*LEF_epochs + 6*barriers*epochs + 8*contacts per launch / launch time",
+                     "traffic_note": "DRAM bytes per launch: ncu bytes per LEF-epoch of a one-wave batched "
+                                     "launch (profiles/simulate_batch_kernel_traffic.json) x this launch's "
+                                     "LEF-epochs; above the algorithmic bytes because the resident cells' "
+                                     "arrays exceed L2",
                      "traffic_over_algorithmic": None},
-        "e2e": e2e, "clocks": clk, "batched": batched, "plain_serial": serial,
+        "e2e": e2e, "clocks": clk, "plain_wave": wave_line, "plain_serial": serial,
     }
     if traffic is not None and agg["bytes"]:
         line["roofline"]["traffic_over_algorithmic"] = traffic * agg["launches"] / agg["bytes"]
         line["roofline"]["captured_launch_lef_epochs_per_s"] = tinfo.get("lef_epochs_per_s")
-    if batched is not None and batched["roofline"]["traffic"] is not None:
-        batched["roofline"]["traffic_over_algorithmic"] = batched["roofline"]["traffic"] / bbytes
-    if batched is not None:
-        line["batched"]["over_plain_wave_cells_per_s"] = batched["cells_per_s"] / line["cells_per_s"]
+    if wave_line is not None:
+        wach = wave_line.pop("bytes") / (wave_line["ms"] / 1e3) / 1e9
+        wtraffic, _ = dram_traffic_per_launch(wagg["lef_epochs"] / max(1, wagg["launches"]))
+        wave_line["roofline"] = {
+            "bound": "hbm", "achieved": wach, "peak": peak, "unit": "GB/s", "frac": wach / peak,
+            "traffic": wtraffic, "peak_source": f"{peak_kind} hbm_gbs", "kernel": "simulate_kernel",
+            "traffic_note": "DRAM bytes per launch: ncu bytes per LEF-epoch of one launch that fills every "
+                            "SM with 24 KiB cells as the concurrent wave does "
+                            "(profiles/simulate_kernel_traffic.json) x this run's LEF-epochs per launch"}
+        wave_line["batched_over_wave_cells_per_s"] = line["cells_per_s"] / wave_line["cells_per_s"]
     if args.windows > 0:
         line["batched_windows"] = run_windows(args, local, log)
     if args.surrogate:
