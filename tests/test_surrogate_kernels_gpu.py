@@ -125,7 +125,7 @@ def test_conv_forward_head_masks_padded_channels(conv_form):
     assert torch.all(buf[B * L * NV:] == 7.0)
 
 
-def test_data_gradient_through_silu_gate():
+def test_data_gradient_through_silu_gate(conv_form):
     """dx = conv(dz, transpose(w)) * silu'(z_prev): the gradient of a SiLU-activated input."""
     rng = np.random.default_rng(12)
     B, L, Cin, Cout = 2, 190, 192, 256
