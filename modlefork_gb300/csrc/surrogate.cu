@@ -70,6 +70,12 @@ struct ConvArgs {
   // shared memory and stores them with TMA.  Maps over [B][L][n_valid] with row stride
   // out_stride and 128-byte swizzled boxes of 32 rows: FP32 boxes of 32 columns, BF16 of 64.
   CUtensorMap tm_f32, tm_pre, tm_post;
+  // fused copies of the post-activation output (staged epilogue only): a second copy into
+  // another row-strided buffer (the skip half of a concatenation), and an upsampled copy, each
+  // output row l stored at rows 2l and 2l + 1 of its buffer (two maps over the even and the odd
+  // rows); out_post may then be null
+  CUtensorMap tm_skip, tm_dup0, tm_dup1;
+  int has_skip, has_dup;
 };
 
 constexpr int STAGE_OUT_BYTES = 4 * 2 * 4096;  // four epilogue warps x two 4 KB buffers
@@ -238,7 +244,7 @@ __device__ void conv_epilogue_staged(const ConvArgs& a, uint32_t tmem_row, uint8
                              pack_bf16x2(v[8 * k + 4], v[8 * k + 5]), pack_bf16x2(v[8 * k + 6], v[8 * k + 7])));
       stage_end(&a.tm_pre, buf, nb, col0, y, z);
     }
-    if (a.out_post) {
+    if (a.out_post || a.has_skip || a.has_dup) {
       if (a.act == MSUR_ACT_SILU) {
 #pragma unroll
         for (int j = 0; j < 64; ++j) v[j] = silu(v[j]);
@@ -249,7 +255,19 @@ __device__ void conv_epilogue_staged(const ConvArgs& a, uint32_t tmem_row, uint8
         stage_put(buf, k,
                   make_uint4(pack_bf16x2(v[8 * k], v[8 * k + 1]), pack_bf16x2(v[8 * k + 2], v[8 * k + 3]),
                              pack_bf16x2(v[8 * k + 4], v[8 * k + 5]), pack_bf16x2(v[8 * k + 6], v[8 * k + 7])));
-      stage_end(&a.tm_post, buf, nb, col0, y, z);
+      // one staged box, stored to every destination of the post-activation value
+      umma::fence_async_smem();
+      __syncwarp();
+      if ((threadIdx.x & 31) == 0) {
+        if (a.out_post) umma::tma_store_3d(&a.tm_post, buf, col0, y, z);
+        if (a.has_skip) umma::tma_store_3d(&a.tm_skip, buf, col0, y, z);
+        if (a.has_dup) {
+          umma::tma_store_3d(&a.tm_dup0, buf, col0, y, z);
+          umma::tma_store_3d(&a.tm_dup1, buf, col0, y, z);
+        }
+        umma::bulk_commit();
+      }
+      ++nb;
     }
   }
 }
@@ -1035,6 +1053,21 @@ int make_out_map(CUtensorMap* m, void* base, CUtensorMapDataType type, int elem_
   return MSUR_OK;
 }
 
+// Map of the upsampled copy: output row l of sequence b at element ((b * 2L + 2l + parity) *
+// row_stride) of base, n_valid columns, boxes of 64 BF16 columns x 32 rows.
+int make_dup_map(CUtensorMap* m, void* base, int parity, int n_valid, int row_stride, int L, int B) {
+  const cuuint64_t gd[3] = {static_cast<cuuint64_t>(n_valid), static_cast<cuuint64_t>(L), static_cast<cuuint64_t>(B)};
+  const cuuint64_t gs[2] = {static_cast<cuuint64_t>(row_stride) * 2 * 2,
+                            static_cast<cuuint64_t>(row_stride) * 2 * 2 * L};
+  const cuuint32_t bx[3] = {64, 32, 1}, es[3] = {1, 1, 1};
+  void* b0 = static_cast<char*>(base) + static_cast<size_t>(parity) * row_stride * 2;
+  const CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, b0, gd, gs, bx, es,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                              CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(MSUR_ERR_CUDA, "cuTensorMapEncodeTiled (upsampled) failed (%d)", static_cast<int>(r));
+  return MSUR_OK;
+}
+
 // Dynamic shared memory of a forward kernel: operand stages, alignment slack, the barriers (a
 // 1 KB block when the staged epilogue's buffers follow it).
 template <int BN, int STAGES, bool STAGED>
@@ -1123,15 +1156,22 @@ int msur_take_error(unsigned* code) {
   return rc;
 }
 
-int msur_conv_forward(const void* x, int B, int L, int Cin, const void* w, int Cout, int taps, const float* bias,
-                      int act, void* out_pre, void* out_post, float* out_f32, int out_stride, int n_valid,
-                      const void* gate, void* stream) {
+static int conv_forward_impl(const void* x, int B, int L, int Cin, const void* w, int Cout, int taps,
+                             const float* bias, int act, void* out_pre, void* out_post, float* out_f32,
+                             int out_stride, int n_valid, const void* gate, void* out_skip, int skip_stride,
+                             void* out_dup, int dup_stride, void* stream) {
   if (!x || !w || B <= 0 || L <= 0 || Cin <= 0 || Cout <= 0 || taps <= 0 || n_valid <= 0 || n_valid > Cout)
     return fail(MSUR_ERR_INVALID_ARG, "msur_conv_forward: bad shape or null pointer");
   if (Cin % BK) return fail(MSUR_ERR_INVALID_ARG, "msur_conv_forward: Cin (%d) must be a multiple of 64", Cin);
   if (taps % 2 == 0) return fail(MSUR_ERR_INVALID_ARG, "msur_conv_forward: taps must be odd");
-  if (!out_pre && !out_post && !out_f32) return fail(MSUR_ERR_INVALID_ARG, "msur_conv_forward: no output");
-  if (out_stride < n_valid || (out_stride % 8) ||
+  if (!out_pre && !out_post && !out_f32 && !out_skip && !out_dup)
+    return fail(MSUR_ERR_INVALID_ARG, "msur_conv_forward: no output");
+  if ((out_skip && (skip_stride < n_valid || (skip_stride % 8) || !aligned16(out_skip))) ||
+      (out_dup && (dup_stride < n_valid || (dup_stride % 8) || !aligned16(out_dup))))
+    return fail(MSUR_ERR_INVALID_ARG,
+                "msur_conv_forward_fused: copies must be 16-byte aligned, their strides multiples of 8 and >= n_valid");
+  const bool primary = out_pre || out_post || out_f32;
+  if ((primary && (out_stride < n_valid || (out_stride % 8))) ||
       !aligned16(x) || !aligned16(w) || (out_pre && !aligned16(out_pre)) || (out_post && !aligned16(out_post)) ||
       (out_f32 && !aligned16(out_f32)) || (gate && !aligned16(gate)))
     return fail(MSUR_ERR_INVALID_ARG, "msur_conv_forward: buffers must be 16-byte aligned, out_stride a multiple of 8");
@@ -1174,17 +1214,40 @@ int msur_conv_forward(const void* x, int B, int L, int Cin, const void* w, int C
   const int form = g_conv_form[slot];
   const bool persistent = (form & 1) != 0;
   const bool staged = (form & 2) != 0 && !gate;
+  if ((out_skip || out_dup) && !staged)
+    return fail(MSUR_ERR_UNSUPPORTED, "msur_conv_forward_fused: the fused copies need the staged form (bit 1) "
+                                      "for N tile %d and no gate", BN);
   if (staged) {
     if (out_f32) rc = make_out_map(&a.tm_f32, out_f32, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, n_valid, out_stride, L, B, 32);
     if (!rc && out_pre)
       rc = make_out_map(&a.tm_pre, out_pre, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, n_valid, out_stride, L, B, 64);
     if (!rc && out_post)
       rc = make_out_map(&a.tm_post, out_post, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, n_valid, out_stride, L, B, 64);
+    if (!rc && out_skip)
+      rc = make_out_map(&a.tm_skip, out_skip, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, n_valid, skip_stride, L, B, 64);
+    if (!rc && out_dup) rc = make_dup_map(&a.tm_dup0, out_dup, 0, n_valid, dup_stride, L, B);
+    if (!rc && out_dup) rc = make_dup_map(&a.tm_dup1, out_dup, 1, n_valid, dup_stride, L, B);
     if (rc) return rc;
+    a.has_skip = out_skip ? 1 : 0;
+    a.has_dup = out_dup ? 1 : 0;
   }
   if (BN == 256) return dispatch_conv<256>(a, ntn, persistent, staged, stages, st);
   if (BN == 128) return dispatch_conv<128>(a, ntn, persistent, staged, stages, st);
   return dispatch_conv<64>(a, ntn, persistent, staged, stages, st);
+}
+
+int msur_conv_forward(const void* x, int B, int L, int Cin, const void* w, int Cout, int taps, const float* bias,
+                      int act, void* out_pre, void* out_post, float* out_f32, int out_stride, int n_valid,
+                      const void* gate, void* stream) {
+  return conv_forward_impl(x, B, L, Cin, w, Cout, taps, bias, act, out_pre, out_post, out_f32, out_stride, n_valid,
+                           gate, nullptr, 0, nullptr, 0, stream);
+}
+
+int msur_conv_forward_fused(const void* x, int B, int L, int Cin, const void* w, int Cout, int taps,
+                            const float* bias, int act, void* out_post, int out_stride, void* out_skip,
+                            int skip_stride, void* out_dup, int dup_stride, int n_valid, void* stream) {
+  return conv_forward_impl(x, B, L, Cin, w, Cout, taps, bias, act, nullptr, out_post, nullptr, out_stride, n_valid,
+                           nullptr, out_skip, skip_stride, out_dup, dup_stride, stream);
 }
 
 int msur_conv_set_stages(int bn, int stages) {

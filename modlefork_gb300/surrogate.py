@@ -202,37 +202,79 @@ class UNet:
         return ws
 
     # ---- forward -------------------------------------------------------------------------
-    def _conv(self, name, x, pre=None, post=None, f32=None, **kw):
-        s = self.specs[name]
+    def _layer_form(self, name):
+        """(form, stages) the convolution `name` runs with: its tuned entry, else the width's."""
         cfg = LAYER_CFG.get(name)
         if cfg is not None:
-            bn = tile_width(s.cout)
+            return cfg
+        bn = tile_width(self.specs[name].cout)
+        return ops.conv_get_form(bn), ops.conv_get_stages(bn)
+
+    def _set_layer(self, name):
+        cfg = LAYER_CFG.get(name)
+        if cfg is not None:
+            bn = tile_width(self.specs[name].cout)
             ops.conv_set_form(bn, cfg[0])
             ops.conv_set_stages(bn, cfg[1])
+
+    def _conv(self, name, x, pre=None, post=None, f32=None, **kw):
+        s = self.specs[name]
+        self._set_layer(name)
         ops.conv_forward(x, self.wb[name], bias=self.b32[name], act=ops.ACT_SILU if s.act else ops.ACT_NONE,
                          out_pre=pre, out_post=post, out_f32=f32, **kw)
 
-    def forward(self, x, train=False, out=None):
+    def _conv_fused(self, name, x, post=None, skip=None, dup=None):
+        s = self.specs[name]
+        self._set_layer(name)
+        ops.conv_forward_fused(x, self.wb[name], bias=self.b32[name], act=ops.ACT_SILU if s.act else ops.ACT_NONE,
+                               out_post=post, skip=skip, dup=dup)
+
+    def fusable(self):
+        """Whether inference can fill the decoder's concatenation buffers from the convolutions
+        that produce them: those convolutions (the encoders' second, the bottleneck's second and
+        the decoders' second above level 0) must run the staged epilogue."""
+        names = [f"enc{i}b" for i in range(self.depth)] + ["mid_b"] + [f"dec{i}b" for i in range(1, self.depth)]
+        return all(self._layer_form(n)[0] & ops.FORM_STAGED for n in names)
+
+    def forward(self, x, train=False, out=None, fuse=True):
         """x: [B, L, 64] BF16 input; returns the [B, L, 600] FP32 prediction: `out` when given
-        (contiguous FP32 on the device), else a workspace view that the next call overwrites."""
+        (contiguous FP32 on the device), else a workspace view that the next call overwrites.
+
+        In inference (and with fuse, when fusable()) the encoder's second convolution also writes
+        its output into the skip half of its level's concatenation buffer, and the convolution
+        below a decoder level writes its output upsampled into the other half, so no separate
+        upsample-and-concatenate step runs; the results are the same either way."""
         B = x.shape[0]
         ws = self._workspace(B, train)
         get = (lambda k: ws.get(k)) if train else (lambda k: None)
+        fused = fuse and not train and self.fusable()
         h = x
         ws["h_in0"] = x
         for i in range(self.depth):
             self._conv(f"enc{i}a", h, pre=get(f"za{i}"), post=ws[f"ya{i}"])
-            self._conv(f"enc{i}b", ws[f"ya{i}"], pre=get(f"zb{i}"), post=ws[f"yb{i}"])
+            if fused:
+                cat = ws[f"cat{i}"]
+                self._conv_fused(f"enc{i}b", ws[f"ya{i}"], post=ws[f"yb{i}"],
+                                 skip=cat[:, :, cat.shape[-1] - self.widths[i]:])
+            else:
+                self._conv(f"enc{i}b", ws[f"ya{i}"], pre=get(f"zb{i}"), post=ws[f"yb{i}"])
             ops.pool2(ws[f"yb{i}"], ws[f"p{i}"])
             h = ws[f"p{i}"]
         self._conv("mid_a", h, pre=get("zma"), post=ws["yma"])
-        self._conv("mid_b", ws["yma"], pre=get("zmb"), post=ws["ymb"])
-        h = ws["ymb"]
+        if fused:
+            self._conv_fused("mid_b", ws["yma"], dup=ws[f"cat{self.depth - 1}"][:, :, :self.mid])
+        else:
+            self._conv("mid_b", ws["yma"], pre=get("zmb"), post=ws["ymb"])
+            h = ws["ymb"]
         for i in reversed(range(self.depth)):
-            ops.upcat(h, ws[f"yb{i}"], ws[f"cat{i}"])
+            if not fused:
+                ops.upcat(h, ws[f"yb{i}"], ws[f"cat{i}"])
             self._conv(f"dec{i}a", ws[f"cat{i}"], pre=get(f"zda{i}"), post=ws[f"yda{i}"])
-            self._conv(f"dec{i}b", ws[f"yda{i}"], pre=get(f"zdb{i}"), post=ws[f"ydb{i}"])
-            h = ws[f"ydb{i}"]
+            if fused and i > 0:
+                self._conv_fused(f"dec{i}b", ws[f"yda{i}"], dup=ws[f"cat{i - 1}"][:, :, :self.widths[i]])
+            else:
+                self._conv(f"dec{i}b", ws[f"yda{i}"], pre=get(f"zdb{i}"), post=ws[f"ydb{i}"])
+                h = ws[f"ydb{i}"]
         dst = ws["out"] if out is None else out
         self._conv("head", h, f32=dst, n_valid=NROWS, out_stride=NROWS)
         return dst

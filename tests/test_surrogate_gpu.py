@@ -85,6 +85,32 @@ def test_full_size_forward_matches_the_fp64_oracle():
     _agree(out, want, "network output")
 
 
+def test_fused_concatenation_equals_the_upcat_path():
+    """Inference with the concatenation buffers filled by the producing convolutions (no upcat
+    step) gives the maps of the unfused forward bit for bit, in the default kernel forms and in
+    the shipped table's."""
+    from modlefork_gb300 import autotune
+
+    rng = np.random.default_rng(4)
+    net = S.UNet(seed=9, head_bias=np.linspace(2, 0, S.NROWS))
+    x = torch.from_numpy(_inputs(rng, 3, net.length)).to(net.dev, torch.bfloat16)
+    saved = {bn: (ops.conv_get_form(bn), ops.conv_get_stages(bn)) for bn in (64, 128, 256)}
+    try:
+        for table in (None, autotune.load_table()):
+            if table:
+                autotune.apply_surrogate(table)
+            assert net.fusable()
+            fused = net.forward(x).clone()
+            plain = net.forward(x, fuse=False).clone()
+            torch.cuda.synchronize()
+            assert torch.equal(fused, plain)
+    finally:
+        S.LAYER_CFG.clear()
+        for bn, (f, st) in saved.items():
+            ops.conv_set_form(bn, f)
+            ops.conv_set_stages(bn, st)
+
+
 def test_host_prediction_path_equals_device_prediction():
     """predict_host (host inputs, host outputs, batches alternating between two device slots with
     the copies back on a second stream, a short last batch) gives the maps predict gives from

@@ -125,6 +125,41 @@ def test_conv_forward_head_masks_padded_channels(conv_form):
     assert torch.all(buf[B * L * NV:] == 7.0)
 
 
+@pytest.mark.parametrize("form", [2, 3], ids=["tile-staged", "persistent-staged"])
+@pytest.mark.parametrize("Cout,C1", [(64, 128), (128, 64), (256, 128)])
+def test_fused_copies_equal_the_post_output(form, Cout, C1):
+    """msur_conv_forward_fused: the post-activation value written as usual, into the skip half of
+    a concatenation buffer, and upsampled by two into the other half of another one, bit for bit
+    what conv_forward writes plus the copies made on the host side; refused without the staged
+    form.  L = 150 leaves a ragged last row tile."""
+    rng = np.random.default_rng(Cout + C1 + form)
+    B, L, Cin = 2, 150, 128
+    x = _bf16(rng.standard_normal((B, L, Cin))).to(DEV)
+    w = _bf16(rng.standard_normal((Cout, 3, Cin)) / 16).to(DEV)
+    bias = torch.from_numpy(rng.standard_normal(Cout).astype(np.float32)).to(DEV)
+    bn = 64 if Cout <= 64 else (256 if Cout % 256 == 0 else 128)
+    saved = ops.conv_get_form(bn)
+    try:
+        ops.conv_set_form(bn, form)
+        want = torch.empty(B, L, Cout, dtype=torch.bfloat16, device=DEV)
+        ops.conv_forward(x, w, bias=bias, act=ops.ACT_SILU, out_post=want)
+        post = torch.full((B, L, Cout), 3.0, dtype=torch.bfloat16, device=DEV)
+        cat = torch.full((B, L, C1 + Cout), 5.0, dtype=torch.bfloat16, device=DEV)
+        up = torch.full((B, 2 * L, Cout + C1), 5.0, dtype=torch.bfloat16, device=DEV)
+        ops.conv_forward_fused(x, w, bias=bias, act=ops.ACT_SILU, out_post=post, skip=cat[:, :, C1:],
+                               dup=up[:, :, :Cout])
+        torch.cuda.synchronize()
+        assert torch.equal(post, want)
+        assert torch.equal(cat[:, :, C1:], want) and torch.all(cat[:, :, :C1] == 5.0)
+        assert torch.equal(up[:, 0::2, :Cout], want) and torch.equal(up[:, 1::2, :Cout], want)
+        assert torch.all(up[:, :, Cout:] == 5.0)
+        ops.conv_set_form(bn, form & 1)
+        with pytest.raises(ops.SurrogateKernelError):
+            ops.conv_forward_fused(x, w, bias=bias, act=ops.ACT_SILU, skip=cat[:, :, C1:])
+    finally:
+        ops.conv_set_form(bn, saved)
+
+
 def test_data_gradient_through_silu_gate(conv_form):
     """dx = conv(dz, transpose(w)) * silu'(z_prev): the gradient of a SiLU-activated input."""
     rng = np.random.default_rng(12)
