@@ -235,20 +235,24 @@ def run_surrogate(args, log):
     pin_track = torch.from_numpy(sims["track"].cpu().numpy()[idx].copy()).pin_memory()
     pin_params = torch.from_numpy(sims["params"].cpu().numpy()[idx].copy()).pin_memory()
     pin_out = torch.empty(B * nbatch, net.length, S.NROWS, dtype=torch.float32).pin_memory()
-    S.predict_host(net, pin_track[:B], pin_params[:B], pin_out[:B], batch=B)  # warm-up
+    S.predict_host(net, pin_track, pin_params, pin_out, batch=B)  # warm-up: every part of the buffers
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     S.predict_host(net, pin_track, pin_params, pin_out, batch=B)
     torch.cuda.synchronize()
     e2e_mps = B * nbatch / (time.perf_counter() - t0)
-    # the link that bounds it: one batch of maps copied device-to-host into the same pinned buffer
-    # (its rate depends on where the host placed the pinned pages, which varies between runs)
+    # the link that bounds it: one batch of maps copied device-to-host into each batch's part of
+    # the same pinned buffer (the rate depends on where the host placed those pinned pages, which
+    # varies between runs and can differ between parts of one large buffer)
     d_maps = torch.empty(B, net.length, S.NROWS, dtype=torch.float32, device=net.dev)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    pin_out[:B].copy_(d_maps, non_blocking=True)
-    torch.cuda.synchronize()
-    d2h_gbs = d_maps.numel() * 4 / (time.perf_counter() - t0) / 1e9
+    d2h_parts = []
+    for k in range(nbatch):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pin_out[k * B:(k + 1) * B].copy_(d_maps, non_blocking=True)
+        torch.cuda.synchronize()
+        d2h_parts.append(d_maps.numel() * 4 / (time.perf_counter() - t0) / 1e9)
+    d2h_gbs = nbatch / sum(1.0 / g for g in d2h_parts)
     del d_maps
     passed = r >= 0.95
     tpeak, tkind = measured_peak("bf16_tflops")
@@ -263,6 +267,7 @@ def run_surrogate(args, log):
                             "launch (CUDA events around the launch)",
         "fp64_target_check_max_rel_dev": sims["fp64_max_rel_dev"],
         "e2e": {"value": e2e_mps, "unit": "maps/s", "batches": nbatch, "d2h_gb_per_s": d2h_gbs,
+                "d2h_gb_per_s_by_batch": d2h_parts,
                 "d2h_bound_maps_per_s": d2h_gbs * 1e9 / (net.length * S.NROWS * 4),
                 "h2d_bytes_per_step": int((pin_track.numel() + pin_params.numel()) * 4) // nbatch,
                 "d2h_bytes_per_step": int(pin_out.numel() * 4) // nbatch},
