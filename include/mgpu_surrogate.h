@@ -55,19 +55,23 @@ int msur_conv_forward(const void* x, int B, int L, int Cin, const void* w, int C
                       const void* gate, void* stream);
 
 /* msur_conv_forward with the post-activation value (act applied; no pre-activation, FP32 or
- * gate) written to up to three places at once, for a U-Net's skip connections:
+ * gate) written to up to four places at once, for a U-Net's skip connections:
  *   out_post [B][L][out_stride] as in msur_conv_forward (or NULL);
  *   out_skip [B][L][skip_stride]: a second copy, e.g. the skip half of a concatenation buffer
  *            (pointer at that half's first channel; or NULL);
  *   out_dup  [B][2L][dup_stride]: nearest upsampling by two, output row l at rows 2l and 2l + 1
- *            (pointer at the first channel of the upsampled half; or NULL).
- * Together with out_skip of the encoder convolution, out_dup of the convolution below a decoder
- * level fills that level's concatenation buffer without msur_upcat.  The copies are TMA stores
- * of the staged epilogue: MSUR_ERR_UNSUPPORTED unless the form of this N tile width has bit 1.
- * Buffers 16-byte aligned, strides multiples of 8 and at least n_valid. */
+ *            (pointer at the first channel of the upsampled half; or NULL);
+ *   out_pool [B][L/2][pool_stride]: average pooling by two of the BF16 values, exactly as
+ *            msur_pool2 computes it (L even; or NULL).
+ * Together with out_skip and out_pool of the encoder convolution, out_dup of the convolution
+ * below a decoder level fills that level's concatenation buffer without msur_upcat or
+ * msur_pool2.  The copies are TMA stores of the staged epilogue: MSUR_ERR_UNSUPPORTED unless
+ * the form of this N tile width has bit 1.  Buffers 16-byte aligned, strides multiples of 8
+ * and at least n_valid. */
 int msur_conv_forward_fused(const void* x, int B, int L, int Cin, const void* w, int Cout, int taps,
                             const float* bias, int act, void* out_post, int out_stride, void* out_skip,
-                            int skip_stride, void* out_dup, int dup_stride, int n_valid, void* stream);
+                            int skip_stride, void* out_dup, int dup_stride, void* out_pool, int pool_stride,
+                            int n_valid, void* stream);
 
 /* Pipeline depth of msur_conv_forward for one N tile width (64, 128 or 256 output channels per
  * tile, chosen by Cout): 2 to 4 shared-memory stages.  Fewer stages let 2-4 CTAs share an SM,

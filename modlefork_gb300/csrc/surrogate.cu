@@ -75,7 +75,10 @@ struct ConvArgs {
   // output row l stored at rows 2l and 2l + 1 of its buffer (two maps over the even and the odd
   // rows); out_post may then be null
   CUtensorMap tm_skip, tm_dup0, tm_dup1;
-  int has_skip, has_dup;
+  // and an average-pooled copy: rows 2m and 2m + 1 (lanes 2m, 2m + 1 of an epilogue warp) into
+  // row m, as msur_pool2 computes it from the BF16 values (16-row boxes)
+  CUtensorMap tm_pool;
+  int has_skip, has_dup, has_pool;
 };
 
 constexpr int STAGE_OUT_BYTES = 4 * 2 * 4096;  // four epilogue warps x two 4 KB buffers
@@ -244,30 +247,55 @@ __device__ void conv_epilogue_staged(const ConvArgs& a, uint32_t tmem_row, uint8
                              pack_bf16x2(v[8 * k + 4], v[8 * k + 5]), pack_bf16x2(v[8 * k + 6], v[8 * k + 7])));
       stage_end(&a.tm_pre, buf, nb, col0, y, z);
     }
-    if (a.out_post || a.has_skip || a.has_dup) {
+    if (a.out_post || a.has_skip || a.has_dup || a.has_pool) {
       if (a.act == MSUR_ACT_SILU) {
 #pragma unroll
         for (int j = 0; j < 64; ++j) v[j] = silu(v[j]);
       }
-      uint8_t* buf = stage_begin(stg, nb);
+      uint32_t pk[32];  // this row's 64 BF16 values in pairs
 #pragma unroll
-      for (int k = 0; k < 8; ++k)
-        stage_put(buf, k,
-                  make_uint4(pack_bf16x2(v[8 * k], v[8 * k + 1]), pack_bf16x2(v[8 * k + 2], v[8 * k + 3]),
-                             pack_bf16x2(v[8 * k + 4], v[8 * k + 5]), pack_bf16x2(v[8 * k + 6], v[8 * k + 7])));
-      // one staged box, stored to every destination of the post-activation value
-      umma::fence_async_smem();
-      __syncwarp();
-      if ((threadIdx.x & 31) == 0) {
-        if (a.out_post) umma::tma_store_3d(&a.tm_post, buf, col0, y, z);
-        if (a.has_skip) umma::tma_store_3d(&a.tm_skip, buf, col0, y, z);
-        if (a.has_dup) {
-          umma::tma_store_3d(&a.tm_dup0, buf, col0, y, z);
-          umma::tma_store_3d(&a.tm_dup1, buf, col0, y, z);
+      for (int j = 0; j < 32; ++j) pk[j] = pack_bf16x2(v[2 * j], v[2 * j + 1]);
+      if (a.out_post || a.has_skip || a.has_dup) {
+        uint8_t* buf = stage_begin(stg, nb);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) stage_put(buf, k, make_uint4(pk[4 * k], pk[4 * k + 1], pk[4 * k + 2], pk[4 * k + 3]));
+        // one staged box, stored to every destination of the post-activation value
+        umma::fence_async_smem();
+        __syncwarp();
+        if ((threadIdx.x & 31) == 0) {
+          if (a.out_post) umma::tma_store_3d(&a.tm_post, buf, col0, y, z);
+          if (a.has_skip) umma::tma_store_3d(&a.tm_skip, buf, col0, y, z);
+          if (a.has_dup) {
+            umma::tma_store_3d(&a.tm_dup0, buf, col0, y, z);
+            umma::tma_store_3d(&a.tm_dup1, buf, col0, y, z);
+          }
+          umma::bulk_commit();
         }
-        umma::bulk_commit();
+        ++nb;
       }
-      ++nb;
+      if (a.has_pool) {
+        // row pairs (2m, 2m + 1) sit on lanes (2m, 2m + 1): the even lane averages them and
+        // writes pooled row m of a 16-row box (y is a multiple of 32)
+        const int lane = threadIdx.x & 31;
+        uint8_t* buf = stage_begin(stg, nb);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          uint32_t q[4];
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            const uint32_t mine = pk[4 * k + h];
+            const uint32_t next = __shfl_down_sync(0xFFFFFFFFu, mine, 1);
+            const float2 fa = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&mine));
+            const float2 fb = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&next));
+            q[h] = pack_bf16x2(0.5f * (fa.x + fb.x), 0.5f * (fa.y + fb.y));
+          }
+          if ((lane & 1) == 0) {
+            const int r = lane >> 1;
+            *reinterpret_cast<uint4*>(buf + r * 128 + ((k ^ (r & 7)) << 4)) = make_uint4(q[0], q[1], q[2], q[3]);
+          }
+        }
+        stage_end(&a.tm_pool, buf, nb, col0, y >> 1, z);
+      }
     }
   }
 }
@@ -1041,11 +1069,11 @@ int make_map(CUtensorMap* m, const void* base, int rank, const uint64_t* dims, c
 // Output map of the staged epilogue: [B][L][n_valid] elements of elem_bytes with row stride
 // out_stride, boxes of box_x columns x 32 rows, 128-byte swizzle.
 int make_out_map(CUtensorMap* m, void* base, CUtensorMapDataType type, int elem_bytes, int n_valid, int out_stride,
-                 int L, int B, int box_x) {
+                 int L, int B, int box_x, int box_rows = 32) {
   const cuuint64_t gd[3] = {static_cast<cuuint64_t>(n_valid), static_cast<cuuint64_t>(L), static_cast<cuuint64_t>(B)};
   const cuuint64_t gs[2] = {static_cast<cuuint64_t>(out_stride) * elem_bytes,
                             static_cast<cuuint64_t>(out_stride) * elem_bytes * L};
-  const cuuint32_t bx[3] = {static_cast<cuuint32_t>(box_x), 32, 1}, es[3] = {1, 1, 1};
+  const cuuint32_t bx[3] = {static_cast<cuuint32_t>(box_x), static_cast<cuuint32_t>(box_rows), 1}, es[3] = {1, 1, 1};
   const CUresult r = g_encode(m, type, 3, base, gd, gs, bx, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                               CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
                               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -1159,15 +1187,17 @@ int msur_take_error(unsigned* code) {
 static int conv_forward_impl(const void* x, int B, int L, int Cin, const void* w, int Cout, int taps,
                              const float* bias, int act, void* out_pre, void* out_post, float* out_f32,
                              int out_stride, int n_valid, const void* gate, void* out_skip, int skip_stride,
-                             void* out_dup, int dup_stride, void* stream) {
+                             void* out_dup, int dup_stride, void* out_pool, int pool_stride, void* stream) {
   if (!x || !w || B <= 0 || L <= 0 || Cin <= 0 || Cout <= 0 || taps <= 0 || n_valid <= 0 || n_valid > Cout)
     return fail(MSUR_ERR_INVALID_ARG, "msur_conv_forward: bad shape or null pointer");
   if (Cin % BK) return fail(MSUR_ERR_INVALID_ARG, "msur_conv_forward: Cin (%d) must be a multiple of 64", Cin);
   if (taps % 2 == 0) return fail(MSUR_ERR_INVALID_ARG, "msur_conv_forward: taps must be odd");
-  if (!out_pre && !out_post && !out_f32 && !out_skip && !out_dup)
+  if (!out_pre && !out_post && !out_f32 && !out_skip && !out_dup && !out_pool)
     return fail(MSUR_ERR_INVALID_ARG, "msur_conv_forward: no output");
+  if (out_pool && (L % 2)) return fail(MSUR_ERR_INVALID_ARG, "msur_conv_forward_fused: pooling needs an even L");
   if ((out_skip && (skip_stride < n_valid || (skip_stride % 8) || !aligned16(out_skip))) ||
-      (out_dup && (dup_stride < n_valid || (dup_stride % 8) || !aligned16(out_dup))))
+      (out_dup && (dup_stride < n_valid || (dup_stride % 8) || !aligned16(out_dup))) ||
+      (out_pool && (pool_stride < n_valid || (pool_stride % 8) || !aligned16(out_pool))))
     return fail(MSUR_ERR_INVALID_ARG,
                 "msur_conv_forward_fused: copies must be 16-byte aligned, their strides multiples of 8 and >= n_valid");
   const bool primary = out_pre || out_post || out_f32;
@@ -1214,7 +1244,7 @@ static int conv_forward_impl(const void* x, int B, int L, int Cin, const void* w
   const int form = g_conv_form[slot];
   const bool persistent = (form & 1) != 0;
   const bool staged = (form & 2) != 0 && !gate;
-  if ((out_skip || out_dup) && !staged)
+  if ((out_skip || out_dup || out_pool) && !staged)
     return fail(MSUR_ERR_UNSUPPORTED, "msur_conv_forward_fused: the fused copies need the staged form (bit 1) "
                                       "for N tile %d and no gate", BN);
   if (staged) {
@@ -1227,9 +1257,13 @@ static int conv_forward_impl(const void* x, int B, int L, int Cin, const void* w
       rc = make_out_map(&a.tm_skip, out_skip, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, n_valid, skip_stride, L, B, 64);
     if (!rc && out_dup) rc = make_dup_map(&a.tm_dup0, out_dup, 0, n_valid, dup_stride, L, B);
     if (!rc && out_dup) rc = make_dup_map(&a.tm_dup1, out_dup, 1, n_valid, dup_stride, L, B);
+    if (!rc && out_pool)
+      rc = make_out_map(&a.tm_pool, out_pool, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, n_valid, pool_stride, L / 2, B, 64,
+                        16);
     if (rc) return rc;
     a.has_skip = out_skip ? 1 : 0;
     a.has_dup = out_dup ? 1 : 0;
+    a.has_pool = out_pool ? 1 : 0;
   }
   if (BN == 256) return dispatch_conv<256>(a, ntn, persistent, staged, stages, st);
   if (BN == 128) return dispatch_conv<128>(a, ntn, persistent, staged, stages, st);
@@ -1240,14 +1274,15 @@ int msur_conv_forward(const void* x, int B, int L, int Cin, const void* w, int C
                       int act, void* out_pre, void* out_post, float* out_f32, int out_stride, int n_valid,
                       const void* gate, void* stream) {
   return conv_forward_impl(x, B, L, Cin, w, Cout, taps, bias, act, out_pre, out_post, out_f32, out_stride, n_valid,
-                           gate, nullptr, 0, nullptr, 0, stream);
+                           gate, nullptr, 0, nullptr, 0, nullptr, 0, stream);
 }
 
 int msur_conv_forward_fused(const void* x, int B, int L, int Cin, const void* w, int Cout, int taps,
                             const float* bias, int act, void* out_post, int out_stride, void* out_skip,
-                            int skip_stride, void* out_dup, int dup_stride, int n_valid, void* stream) {
+                            int skip_stride, void* out_dup, int dup_stride, void* out_pool, int pool_stride,
+                            int n_valid, void* stream) {
   return conv_forward_impl(x, B, L, Cin, w, Cout, taps, bias, act, nullptr, out_post, nullptr, out_stride, n_valid,
-                           nullptr, out_skip, skip_stride, out_dup, dup_stride, stream);
+                           nullptr, out_skip, skip_stride, out_dup, dup_stride, out_pool, pool_stride, stream);
 }
 
 int msur_conv_set_stages(int bn, int stages) {

@@ -223,11 +223,11 @@ class UNet:
         ops.conv_forward(x, self.wb[name], bias=self.b32[name], act=ops.ACT_SILU if s.act else ops.ACT_NONE,
                          out_pre=pre, out_post=post, out_f32=f32, **kw)
 
-    def _conv_fused(self, name, x, post=None, skip=None, dup=None):
+    def _conv_fused(self, name, x, post=None, skip=None, dup=None, pool=None):
         s = self.specs[name]
         self._set_layer(name)
         ops.conv_forward_fused(x, self.wb[name], bias=self.b32[name], act=ops.ACT_SILU if s.act else ops.ACT_NONE,
-                               out_post=post, skip=skip, dup=dup)
+                               out_post=post, skip=skip, dup=dup, pool=pool)
 
     def fusable(self):
         """Whether inference can fill the decoder's concatenation buffers from the convolutions
@@ -240,10 +240,11 @@ class UNet:
         """x: [B, L, 64] BF16 input; returns the [B, L, 600] FP32 prediction: `out` when given
         (contiguous FP32 on the device), else a workspace view that the next call overwrites.
 
-        In inference (and with fuse, when fusable()) the encoder's second convolution also writes
-        its output into the skip half of its level's concatenation buffer, and the convolution
-        below a decoder level writes its output upsampled into the other half, so no separate
-        upsample-and-concatenate step runs; the results are the same either way."""
+        In inference (and with fuse, when fusable()) the encoder's second convolution writes its
+        output into the skip half of its level's concatenation buffer and, pooled, into the next
+        level's input, and the convolution below a decoder level writes its output upsampled into
+        the other half, so no separate pooling or upsample-and-concatenate step runs; the results
+        are the same either way."""
         B = x.shape[0]
         ws = self._workspace(B, train)
         get = (lambda k: ws.get(k)) if train else (lambda k: None)
@@ -254,11 +255,11 @@ class UNet:
             self._conv(f"enc{i}a", h, pre=get(f"za{i}"), post=ws[f"ya{i}"])
             if fused:
                 cat = ws[f"cat{i}"]
-                self._conv_fused(f"enc{i}b", ws[f"ya{i}"], post=ws[f"yb{i}"],
-                                 skip=cat[:, :, cat.shape[-1] - self.widths[i]:])
+                self._conv_fused(f"enc{i}b", ws[f"ya{i}"], skip=cat[:, :, cat.shape[-1] - self.widths[i]:],
+                                 pool=ws[f"p{i}"])
             else:
                 self._conv(f"enc{i}b", ws[f"ya{i}"], pre=get(f"zb{i}"), post=ws[f"yb{i}"])
-            ops.pool2(ws[f"yb{i}"], ws[f"p{i}"])
+                ops.pool2(ws[f"yb{i}"], ws[f"p{i}"])
             h = ws[f"p{i}"]
         self._conv("mid_a", h, pre=get("zma"), post=ws["yma"])
         if fused:

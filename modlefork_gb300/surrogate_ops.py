@@ -49,7 +49,8 @@ def load(path=LIB_PATH):
         "msur_conv_set_stages": (i32, [i32, i32]),
         "msur_conv_get_stages": (i32, [i32]),
         "msur_conv_forward_fused": (i32, [C.c_void_p, i32, i32, i32, C.c_void_p, i32, i32, C.c_void_p, i32,
-                                           C.c_void_p, i32, C.c_void_p, i32, C.c_void_p, i32, i32, C.c_void_p]),
+                                           C.c_void_p, i32, C.c_void_p, i32, C.c_void_p, i32, C.c_void_p, i32,
+                                           i32, C.c_void_p]),
         "msur_conv_set_form": (i32, [i32, i32]),
         "msur_conv_get_form": (i32, [i32]),
         "msur_conv_set_persistent": (i32, [i32, i32]),
@@ -99,20 +100,21 @@ def conv_forward(x, w, bias=None, act=ACT_NONE, out_pre=None, out_post=None, out
                                     _p(out_f32), out_stride, n_valid, _p(gate), _stream()), "msur_conv_forward")
 
 
-def conv_forward_fused(x, w, bias=None, act=ACT_NONE, out_post=None, skip=None, dup=None):
+def conv_forward_fused(x, w, bias=None, act=ACT_NONE, out_post=None, skip=None, dup=None, pool=None):
     """conv_forward's post-activation value written to out_post [B, L, Cout] (or None), to the
-    row-strided view `skip` [B, L, Cout] (e.g. cat[:, :, C1:]) and, upsampled by two, to the
-    row-strided view `dup` [B, 2L, Cout] (e.g. cat[:, :, :C1]); needs the staged kernel form."""
+    row-strided view `skip` [B, L, Cout] (e.g. cat[:, :, C1:]), upsampled by two to the
+    row-strided view `dup` [B, 2L, Cout] (e.g. cat[:, :, :C1]) and average-pooled by two to
+    `pool` [B, L/2, Cout] (as pool2 computes it); needs the staged kernel form."""
     B, L, Cin = x.shape
     Cout, taps, _ = w.shape
-    for t, rows in ((skip, L), (dup, 2 * L)):
+    for t, rows in ((skip, L), (dup, 2 * L), (pool, L // 2)):
         if t is not None:
             assert t.shape == (B, rows, Cout) and t.stride(2) == 1 and t.stride(0) == rows * t.stride(1)
     out_stride = out_post.shape[-1] if out_post is not None else Cout
+    stride = lambda t: t.stride(1) if t is not None else 0  # noqa: E731
     _check(load().msur_conv_forward_fused(
-        _p(x), B, L, Cin, _p(w), Cout, taps, _p(bias), act, _p(out_post), out_stride, _p(skip),
-        skip.stride(1) if skip is not None else 0, _p(dup), dup.stride(1) if dup is not None else 0, Cout,
-        _stream()), "msur_conv_forward_fused")
+        _p(x), B, L, Cin, _p(w), Cout, taps, _p(bias), act, _p(out_post), out_stride, _p(skip), stride(skip),
+        _p(dup), stride(dup), _p(pool), stride(pool), Cout, _stream()), "msur_conv_forward_fused")
 
 
 def conv_wgrad(x, dz, dw, splits=0):

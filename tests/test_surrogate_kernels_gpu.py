@@ -129,9 +129,9 @@ def test_conv_forward_head_masks_padded_channels(conv_form):
 @pytest.mark.parametrize("Cout,C1", [(64, 128), (128, 64), (256, 128)])
 def test_fused_copies_equal_the_post_output(form, Cout, C1):
     """msur_conv_forward_fused: the post-activation value written as usual, into the skip half of
-    a concatenation buffer, and upsampled by two into the other half of another one, bit for bit
-    what conv_forward writes plus the copies made on the host side; refused without the staged
-    form.  L = 150 leaves a ragged last row tile."""
+    a concatenation buffer, upsampled by two into the other half of another one and average-pooled
+    by two, bit for bit what conv_forward writes plus the copies and the pooling made separately;
+    refused without the staged form.  L = 150 leaves a ragged last row tile (and a pooled one)."""
     rng = np.random.default_rng(Cout + C1 + form)
     B, L, Cin = 2, 150, 128
     x = _bf16(rng.standard_normal((B, L, Cin))).to(DEV)
@@ -146,10 +146,14 @@ def test_fused_copies_equal_the_post_output(form, Cout, C1):
         post = torch.full((B, L, Cout), 3.0, dtype=torch.bfloat16, device=DEV)
         cat = torch.full((B, L, C1 + Cout), 5.0, dtype=torch.bfloat16, device=DEV)
         up = torch.full((B, 2 * L, Cout + C1), 5.0, dtype=torch.bfloat16, device=DEV)
+        pooled = torch.full((B, L // 2, Cout), 5.0, dtype=torch.bfloat16, device=DEV)
+        want_pool = torch.empty_like(pooled)
+        ops.pool2(want, want_pool)
         ops.conv_forward_fused(x, w, bias=bias, act=ops.ACT_SILU, out_post=post, skip=cat[:, :, C1:],
-                               dup=up[:, :, :Cout])
+                               dup=up[:, :, :Cout], pool=pooled)
         torch.cuda.synchronize()
         assert torch.equal(post, want)
+        assert torch.equal(pooled, want_pool)
         assert torch.equal(cat[:, :, C1:], want) and torch.all(cat[:, :, :C1] == 5.0)
         assert torch.equal(up[:, 0::2, :Cout], want) and torch.equal(up[:, 1::2, :Cout], want)
         assert torch.all(up[:, :, Cout:] == 5.0)
