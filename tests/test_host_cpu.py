@@ -192,3 +192,23 @@ def test_launch_setting_layout_and_surrogate_library_exports():
     assert surrogate_ops.conv_get_form(128) == 3 and surrogate_ops.conv_get_persistent(128) == 1
     surrogate_ops.conv_set_form(128, surrogate_ops.FORM_STAGED)
     assert surrogate_ops.conv_get_persistent(128) == 0
+
+
+def test_fused_convolution_arguments_are_checked_before_device_work():
+    """msur_conv_forward_fused refuses odd lengths for pooling, unaligned copies and short
+    strides with MSUR_ERR_INVALID_ARG before it touches a device (fake aligned addresses)."""
+    from modlefork_gb300 import surrogate_ops
+
+    lib = surrogate_ops.load()
+    X, W, OUT = 1 << 20, 2 << 20, 3 << 20  # 16-byte aligned, never dereferenced
+
+    def call(L=128, out_skip=0, skip_stride=0, out_dup=0, dup_stride=0, out_pool=0, pool_stride=0):
+        return lib.msur_conv_forward_fused(X, 2, L, 64, W, 64, 3, None, 1, None, 64, out_skip or None, skip_stride,
+                                           out_dup or None, dup_stride, out_pool or None, pool_stride, 64, None)
+
+    invalid = -1  # MSUR_ERR_INVALID_ARG
+    assert call(L=127, out_pool=OUT, pool_stride=64) == invalid          # pooling needs an even L
+    assert call(out_skip=OUT + 8, skip_stride=64) == invalid            # unaligned copy
+    assert call(out_dup=OUT, dup_stride=60) == invalid                  # stride not a multiple of 8
+    assert call(out_pool=OUT, pool_stride=32) == invalid                # stride below n_valid
+    assert call() == invalid                                            # no output at all
