@@ -13,6 +13,12 @@
 // come back as zeros, which is the convolution's zero padding.  The data gradient is the same
 // product with the taps reversed and W transposed; the weight gradient contracts over the
 // positions (K = B x L) with both operands M/N-major.
+//
+// The forward kernels come in four forms (one CTA per tile or persistent; per-thread output
+// rows or a staged epilogue that writes 32-row boxes to shared memory and stores them with
+// TMA).  The staged epilogue can store the same box to several places at once, which lets a
+// U-Net's convolutions fill their skip concatenations, upsampled halves and pooled inputs
+// directly (msur_conv_forward_fused).
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
